@@ -1,0 +1,339 @@
+"""Benchmark: Msamples/s of the plain megakernel on the 1080p instanced-mesh
+scene (8 BLAS of 10k-80k triangles, 256 instances, 4 textures, one emissive
+quad, 1920x1080, 256 spp, depth 8), on 1..N GB300s.
+
+One step = one PathTracer.render() of `--spp` sample passes (default 256,
+the configuration's sample count) continuing the progressive render.
+
+  value    Msamples/s with the scene and targets resident in HBM; device time
+           of each step from CUDA events on the library's stream; L2 is
+           flushed (a 256 MiB write) between timed steps, outside the events.
+  e2e      the same metric through the C ABI as an application uses it:
+           orn_render + orn_get_framebuffer into pinned host memory each step
+           (the 144-byte ConstantParams go host-to-device with the launch; the
+           1080p RGBA32F framebuffer comes back), timed by CUDA events.
+  roofline algorithmic bytes per megakernel launch from exact work counters
+           of one extra (untimed) step — node visits, leaf transforms, hit
+           shading gathers, per-sample buffer traffic — divided by the
+           average launch time, against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU restatement of the reference (oracle/oracle.cpp, all
+           host threads) on a bounded sample of the same workload.
+
+`--impl reference` times the reference implementation of the path on the
+host cores (the CPU restatement, pinned bit-for-bit to the reference's own
+kernels) on the same workload sample; it runs on rank 0 only.
+
+Multi-GPU: one process per GPU (torchrun); every rank renders its own copy
+of the frame (replicas: pixels and samples are independent, no exchange);
+value = all ranks' samples / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Msamples/s at 1080p"
+UNIT = "Msamples/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--spp", type=int, default=256, help="sample passes per step (render iterations)")
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--depth", type=int, default=8)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(args):
+    from zig_ornament_gb300 import scenes, ornament
+    scene = scenes.instanced_meshes_scene(args.width, args.height)
+    bvh = ornament.Bvh(scene)
+    tris = sum(len(m.vertex_indices) // 3 for m in scene.meshes)
+    cfg = {"workload": "instanced meshes TLAS/BLAS: 8 BLAS icospheres+tori 10k-80k tris, 256 instances, "
+                       "4 procedural 1024^2 RGBA8 textures, 1 emissive quad (radiance 15)",
+           "resolution": f"{args.width}x{args.height}", "spp_per_step": args.spp, "depth": args.depth,
+           "triangles": tris, "instances": len(scene.mesh_instances), "blas": len(scene.meshes),
+           "tlas_nodes": int(len(bvh.tlas_nodes)), "blas_nodes": int(len(bvh.blas_nodes)),
+           "kernel": "plain megakernel (one thread per pixel, passes looped in-thread)",
+           "semantics": "HIP", "transcendentals": "portable (bit-exact with the CPU oracle)",
+           "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
+    return scene, bvh, cfg
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes(c):
+    """Bytes the algorithm touches, from exact work counters (per the
+    reference's data layout): 64 B per node visit, 64 B inverse transform per
+    sphere-leaf test and per mesh entry, 32 B material per hit, 64 B forward
+    transform per sphere hit, 96 B index/normal/uv gathers plus a 64 B
+    inverse transform per mesh hit, 4 B per textured hit, and per sample
+    16 B accumulation read + 16 B write + 8 B RNG read/write + 16 B
+    framebuffer."""
+    hits = c["sphere_hits"] + c["mesh_hits"]
+    return (64 * c["visits"] + 64 * (c["sphere_leaf"] + c["mesh_entry"]) + 32 * hits + 64 * c["sphere_hits"]
+            + (96 + 64) * c["mesh_hits"] + 4 * c["textured_hits"] + 56 * c["samples"])
+
+
+def cpu_baseline(bvh, scene, args, seconds, threads=0):
+    """The CPU restatement on the host cores over a stripe of pixels sized
+    for about `seconds` of work; returns (Msamples/s, threads, description)."""
+    from oracle import oracle_lib as ol
+    oracle = ol.Oracle()
+    cp = ol.make_params(scene.camera, args.width, args.height, depth=args.depth,
+                        textures_count=bvh.scene_textures_count)
+    n = args.width * args.height
+    nthreads = threads or os.cpu_count() or 1
+    # calibrate on a small stripe in the middle of the frame
+    lo = n // 2 - 4096
+    t0 = time.perf_counter()
+    oracle.render(bvh, cp, 1, pixel_range=(lo, lo + 8192), threads=nthreads)
+    rate = 8192 / max(time.perf_counter() - t0, 1e-6)
+    spp = 4
+    pixels = int(min(n, max(16384, rate * seconds / spp)))
+    lo = max(0, (n - pixels) // 2)
+    t0 = time.perf_counter()
+    oracle.render(bvh, cp, spp, pixel_range=(lo, lo + pixels), threads=nthreads)
+    dt = time.perf_counter() - t0
+    value = pixels * spp / dt / 1e6
+    return value, nthreads, f"{pixels} pixels (rows around the frame centre) x {spp} spp, {dt:.1f} s"
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    scene, bvh, cfg = workload(args)
+    vals = []
+    desc = ""
+    for i in range(args.warmup + args.steps):
+        v, cores, desc = cpu_baseline(bvh, scene, args, max(2.0, args.cpu_seconds / 3))
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "per step: " + desc + "; the CPU restatement of the reference's HIP "
+                                       "kernels (bit-exact with them), OpenMP over pixels"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from zig_ornament_gb300 import _lib, ornament
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    scene, bvh, cfg = workload(args)
+    r = ornament.Renderer(bvh, device=local)
+    r.set_resolution(args.width, args.height)
+    st = _lib.State()
+    st.depth, st.flip_y, st.inverted_gamma, st.iterations = args.depth, 0, 1.0, args.spp
+    st.ray_cast_epsilon, st.semantics, st.kernel, st.spp_per_launch = 0.001, 0, 0, 0
+    r.set_state(st)
+    r.set_camera(scene.camera.to_struct())
+    stream = torch.cuda.ExternalStream(r.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    n_px = args.width * args.height
+    fb_host = torch.empty((n_px, 4), dtype=torch.float32, pin_memory=True)
+    fb_np = fb_host.numpy()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(args.warmup):
+        r.render()
+        flush_l2()
+    r.synchronize()
+    launches0 = r.launch_count()
+    barrier()
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r.render()
+            e1.record(stream)
+            flush_l2()
+            times.append((e0, e1))
+        r.synchronize()
+        torch.cuda.synchronize()
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in times]
+    launches = r.launch_count() - launches0
+    # e2e: render + framebuffer readback through the C ABI, host buffers
+    e2e_times = []
+    for _ in range(args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.render()
+        r.framebuffer(fb_np)
+        e1.record(stream)
+        flush_l2()
+        e2e_times.append((e0, e1))
+    r.synchronize()
+    e2e_ms = [a.elapsed_time(b) for a, b in e2e_times]
+    # exact work of one step (untimed)
+    r.enable_counters(True)
+    r.render()
+    counters = r.counters()
+    r.enable_counters(False)
+    launches_per_step = launches / args.steps
+    samples_step = n_px * args.spp
+    total_ms = float(sum(step_ms))
+    total_e2e = float(sum(e2e_ms))
+    if dist:
+        t = torch.tensor([total_ms, total_e2e], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, total_e2e = float(t[0]), float(t[1])
+    value = world * samples_step * args.steps / (total_ms / 1e3) / 1e6
+    e2e_value = world * samples_step * args.steps / (total_e2e / 1e3) / 1e6
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = measured_peaks()
+    avg_launch_s = (sum(step_ms) / 1e3) / max(launches, 1)
+    bytes_per_launch = algorithmic_bytes(counters) / max(launches_per_step, 1)
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "mega_kernel_dram_traffic.json"
+    if tp.exists():
+        try:
+            traffic = json.loads(tp.read_text()).get("bytes_per_launch_at_bench_size")
+        except ValueError:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": cfg,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 144 * launches_per_step,
+                "d2h_bytes_per_step": n_px * 16},
+        "gpu_launches": int(launches),
+        "rays_per_s": counters["rays"] / samples_step * value * 1e6,
+        "work_per_step": counters,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} HBM copy",
+                     "note": "algorithmic bytes mostly hit L1/L2: the traversal working set is L2-resident"},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        v, cores, desc = cpu_baseline(bvh, scene, args, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": desc + "; CPU restatement of the reference (bit-exact with its own "
+                                          "kernels compiled for the host)"}
+    print(json.dumps(line), flush=True)
+    r.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

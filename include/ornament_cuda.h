@@ -1,0 +1,354 @@
+/*
+ * ornament_cuda.h — C ABI of libornament_cuda, a GB300 (sm_103a) path-tracing
+ * backend for the zig_ornament scene model.
+ *
+ * The library replaces the two GPU backends of zig_ornament
+ * (src/wgpu_backend/path_tracer.zig, src/hip_backend/path_tracer.zig) behind
+ * the same duck-typed PathTracer surface: init / deinit / setResolution /
+ * render / getFrameBuffer, with the public `state` and `scene.camera` fields
+ * mapped to orn_set_state / orn_set_camera.  Every entry point below names
+ * the reference function it replaces as `file:line` (paths inside the
+ * zig_ornament project).
+ *
+ * Conventions
+ *   - Plain C types only; every call returns an int status (ORN_OK = 0).
+ *     The library never aborts; orn_last_error() gives a message.
+ *   - One context per host thread.  orn_render() is asynchronous on the
+ *     context's own CUDA stream; every orn_get_* call synchronises.
+ *   - Struct layouts are byte-identical to src/gpu_structs.zig (checked by
+ *     static asserts in the library and by the Python binding).
+ */
+#ifndef ORNAMENT_CUDA_H
+#define ORNAMENT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORN_ABI_VERSION 1u
+
+/* ---- status codes ------------------------------------------------------ */
+enum orn_status {
+    ORN_OK = 0,
+    ORN_ERR_INVALID_ARGUMENT = 1, /* null pointer, zero size, bad enum      */
+    ORN_ERR_EMPTY_SCENE = 2,      /* src/bvh.zig:35-37 panics; we return    */
+    ORN_ERR_OUT_OF_MEMORY = 3,    /* host or device allocation failed       */
+    ORN_ERR_CUDA = 4,             /* a CUDA runtime call failed             */
+    ORN_ERR_NO_DEVICE = 5,        /* no CUDA device / bad device ordinal    */
+    ORN_ERR_BAD_SCENE = 6,        /* an index in the scene is out of range  */
+    ORN_ERR_STACK_OVERFLOW = 7,   /* a ray needed more than 64 stack slots  */
+    ORN_ERR_BUFFER_TOO_SMALL = 8, /* destination smaller than the target    */
+    ORN_ERR_TIMEOUT = 9           /* a bounded device-side wait gave up     */
+};
+
+/* ---- GPU data layouts (src/gpu_structs.zig) ---------------------------- */
+
+/* BvhNodeType, src/gpu_structs.zig:15-20 */
+enum orn_node_type {
+    ORN_NODE_INTERNAL = 0,
+    ORN_NODE_SPHERE = 1,
+    ORN_NODE_MESH = 2,
+    ORN_NODE_TRIANGLE = 3
+};
+
+/* BvhNode, src/gpu_structs.zig:22-31 — 64 bytes. */
+typedef struct orn_bvh_node {
+    float left_aabb_min_or_v0[3];
+    uint32_t left_or_custom_id;
+    float left_aabb_max_or_v1[3];
+    uint32_t right_or_material_index;
+    float right_aabb_min_or_v2[3];
+    uint32_t node_type;
+    float right_aabb_max_or_v3[3];
+    uint32_t transform_id;
+} orn_bvh_node;
+
+/* MaterialType, src/material.zig:4-9 */
+enum orn_material_type {
+    ORN_LAMBERTIAN = 0,
+    ORN_METAL = 1,
+    ORN_DIELECTRIC = 2,
+    ORN_DIFFUSE_LIGHT = 3
+};
+
+#define ORN_NO_TEXTURE 0xFFFFFFFFu
+
+/* Material, src/gpu_structs.zig:33-59 — 32 bytes. */
+typedef struct orn_material {
+    float albedo[3];
+    uint32_t albedo_texture_index; /* ORN_NO_TEXTURE = plain albedo */
+    float fuzz;
+    float ior;
+    uint32_t type; /* enum orn_material_type */
+    uint32_t _padding;
+} orn_material;
+
+/* Camera, src/gpu_structs.zig:88-117 — 112 bytes. */
+typedef struct orn_camera {
+    float origin[3];
+    float lens_radius;
+    float lower_left_corner[3];
+    uint32_t _padding0;
+    float horizontal[3];
+    uint32_t _padding1;
+    float vertical[3];
+    uint32_t _padding2;
+    float u[3];
+    uint32_t _padding3;
+    float v[3];
+    uint32_t _padding4;
+    float w[3];
+    uint32_t _padding5;
+} orn_camera;
+
+/* ConstantParams, src/gpu_structs.zig:61-86 — 144 bytes. */
+typedef struct orn_constant_params {
+    orn_camera camera;
+    uint32_t depth;
+    uint32_t width;
+    uint32_t height;
+    uint32_t flip_y;
+    float inverted_gamma;
+    float ray_cast_epsilon;
+    uint32_t textures_count;
+    float current_iteration;
+} orn_constant_params;
+
+/* Texture texel formats.  RGBA8 unorm is the LDR path of both backends
+ * (src/hip_backend/buffers.zig:106, src/wgpu_backend/buffers.zig:305-319);
+ * RGBA16F is the wgpu HDR path (rgba16_float). */
+enum orn_texel_format { ORN_TEXEL_RGBA8 = 0, ORN_TEXEL_RGBA16F = 1 };
+
+/* One texture (src/texture.zig:3-14).  Rows are `bytes_per_row` apart;
+ * the data is copied at orn_create time. */
+typedef struct orn_texture {
+    const void* data;
+    uint32_t width;
+    uint32_t height;
+    uint32_t bytes_per_row;
+    uint32_t format; /* enum orn_texel_format */
+} orn_texture;
+
+/* The flat arrays that Bvh.init returns (src/bvh.zig:22-31), in the HIP
+ * layout: `transforms` hold the TRANSPOSE of each zmath matrix
+ * (row_major_transforms = true, src/bvh.zig:364-367), pairs
+ * {inverse, forward} indexed transform_id*2 and transform_id*2+1. */
+typedef struct orn_scene_blob {
+    const orn_bvh_node* tlas_nodes;  uint32_t tlas_nodes_len;
+    const orn_bvh_node* blas_nodes;  uint32_t blas_nodes_len;
+    const float* normals;            uint32_t normals_len;        /* 4 floats each */
+    const uint32_t* normal_indices;  uint32_t normal_indices_len;
+    const float* uvs;                uint32_t uvs_len;            /* 2 floats each */
+    const uint32_t* uv_indices;      uint32_t uv_indices_len;
+    const float* transforms;         uint32_t transforms_len;     /* 16 floats each */
+    const orn_material* materials;   uint32_t materials_len;
+    const orn_texture* textures;     uint32_t textures_len;
+    /* scene.textures.items.len (src/hip_backend/path_tracer.zig:165): the
+     * value written to ConstantParams.textures_count. */
+    uint32_t scene_textures_count;
+} orn_scene_blob;
+
+/* Which backend's semantics to reproduce where the two differ:
+ * metal absorption (src/wgpu_backend/shaders/material.wgsl:22-27 vs
+ * src/hip_backend/kernels/material.hip.h:58-64) and the texture address
+ * mode (clamp-to-edge for wgpu's default sampler, wrap for HIP). */
+enum orn_semantics { ORN_SEMANTICS_HIP = 0, ORN_SEMANTICS_WGSL = 1 };
+
+/* Kernel variant used by orn_render. */
+enum orn_kernel {
+    ORN_KERNEL_MEGA = 0,      /* one thread per pixel, samples looped in-thread */
+    ORN_KERNEL_WAVEFRONT = 1  /* persistent path pool + compacted ray queues   */
+};
+
+/* State, src/state.zig:3-23 (resolution set by orn_set_resolution). */
+typedef struct orn_state {
+    uint32_t depth;           /* default 10   */
+    uint32_t flip_y;          /* default 0    */
+    float inverted_gamma;     /* default 1    */
+    uint32_t iterations;      /* default 1    */
+    float ray_cast_epsilon;   /* default 1e-3 */
+    uint32_t semantics;       /* enum orn_semantics, default HIP */
+    uint32_t kernel;          /* enum orn_kernel, default MEGA   */
+    uint32_t spp_per_launch;  /* 0 = library chooses             */
+} orn_state;
+
+/* A ray for orn_trace_rays (src/hip_backend/kernels/ray.hip.h:7-18). */
+typedef struct orn_ray {
+    float origin[3];
+    float direction[3];
+} orn_ray;
+
+/* The closest hit that Bvh::hit reports through its out-parameters
+ * (src/hip_backend/kernels/bvh.hip.h:145-152).  Fields other than `hit`
+ * keep the value 0 when hit == 0; tri_id and uv keep 0 for sphere hits. */
+typedef struct orn_hit {
+    uint32_t hit;
+    float t;
+    uint32_t material_index;
+    uint32_t node_type;             /* ORN_NODE_SPHERE or ORN_NODE_MESH */
+    uint32_t inverted_transform_id; /* identifies the instance          */
+    uint32_t tri_id;                /* 3 * global triangle index        */
+    float uv[2];
+} orn_hit;
+
+typedef struct orn_context orn_context;
+
+/* ---- context life cycle ------------------------------------------------- */
+
+/* PathTracer.init — src/hip_backend/path_tracer.zig:36-86.  Copies every
+ * blob array to device `device` (-1 = the last device, as the HIP backend
+ * picks, src/hip_backend/path_tracer.zig:40).  The caller keeps ownership
+ * of the blob.  Validates every index in the blob. */
+int orn_create(const orn_scene_blob* blob, int device, orn_context** out);
+
+/* PathTracer.deinit — src/hip_backend/path_tracer.zig:88-101. */
+int orn_destroy(orn_context* ctx);
+
+/* State setters (src/state.zig:25-71).  Returns the defaults of
+ * State.init (src/state.zig:13-23) before the first set. */
+int orn_set_state(orn_context* ctx, const orn_state* state);
+int orn_get_state(const orn_context* ctx, orn_state* out);
+
+/* Assigning scene.camera / Camera.setLookAt / setAspectRatio sets the
+ * camera dirty flag (src/camera.zig:66,70-80,98-113); the next render
+ * restarts accumulation (src/hip_backend/path_tracer.zig:150-158). */
+int orn_set_camera(orn_context* ctx, const orn_camera* camera);
+
+/* PathTracer.setResolution — src/hip_backend/path_tracer.zig:103-109.
+ * Drops the target buffers; the next render re-creates them and reseeds
+ * every pixel's RNG state with its pixel index. */
+int orn_set_resolution(orn_context* ctx, uint32_t width, uint32_t height);
+int orn_get_resolution(const orn_context* ctx, uint32_t* width, uint32_t* height);
+
+/* PathTracer.render — src/hip_backend/path_tracer.zig:121-133:
+ * `iterations` sample passes then post-processing.  Asynchronous. */
+int orn_render(orn_context* ctx);
+
+/* Blocks until all work queued on the context has finished. */
+int orn_synchronize(orn_context* ctx);
+
+/* PathTracer.getFrameBuffer — src/hip_backend/path_tracer.zig:111-119.
+ * `dst` holds pixel_count RGBA float4 values (16 bytes each). */
+int orn_get_framebuffer(orn_context* ctx, float* dst, size_t pixel_count);
+
+/* The FP32 RGBA accumulation buffer (not exposed by the reference; used
+ * for checkpointing and parity tests). */
+int orn_get_accumulation(orn_context* ctx, float* dst, size_t pixel_count);
+
+/* Checkpoint / resume of the progressive state: accumulation buffer,
+ * per-pixel RNG states and State.current_iteration. */
+int orn_get_progress(orn_context* ctx, float* accumulation, uint32_t* rng_state,
+                     size_t pixel_count, float* current_iteration);
+int orn_set_progress(orn_context* ctx, const float* accumulation,
+                     const uint32_t* rng_state, size_t pixel_count,
+                     float current_iteration);
+
+/* The ConstantParams the next sample pass would use (after applying the
+ * camera dirty flag), for parity checks.  Does not change the state. */
+int orn_peek_constant_params(const orn_context* ctx, orn_constant_params* out);
+
+/* ---- parity / debugging ------------------------------------------------- */
+
+/* Bvh::hit on a list of rays — src/hip_backend/kernels/bvh.hip.h:145-276.
+ * Writes one orn_hit per ray and, if `visits` is not NULL, the number of
+ * traversal-loop iterations (node visits) each ray took.  Synchronous. */
+int orn_trace_rays(orn_context* ctx, const orn_ray* rays, size_t count,
+                   orn_hit* hits, uint32_t* visits);
+
+/* Work counters of the last orn_render (zeros unless enabled with
+ * orn_enable_counters): [0] samples, [1] extension rays, [2] node visits,
+ * [3] internal-node visits, [4] sphere-leaf visits, [5] mesh-entry visits,
+ * [6] triangle visits, [7] sphere hits, [8] mesh hits, [9] textured hits. */
+#define ORN_COUNTER_COUNT 10
+int orn_enable_counters(orn_context* ctx, int enable);
+int orn_get_counters(orn_context* ctx, uint64_t* out, size_t count);
+
+/* Device-side kernel time of the last orn_render in milliseconds (CUDA
+ * events on the context stream). */
+int orn_last_render_ms(orn_context* ctx, float* ms);
+
+/* The context's CUDA stream (a cudaStream_t), so a caller can order its own
+ * work and CUDA events with the library's. */
+int orn_get_stream(const orn_context* ctx, void** stream);
+
+/* Number of kernel launches the context has issued since creation. */
+int orn_launch_count(const orn_context* ctx, uint64_t* launches);
+
+/* ---- errors ------------------------------------------------------------- */
+const char* orn_last_error(const orn_context* ctx);
+const char* orn_status_string(int status);
+uint32_t orn_abi_version(void);
+
+/* ---- BVH builder (src/bvh.zig:33-78 Bvh.init) ----------------------------
+ * Builds the flat TLAS/BLAS arrays from a scene description with the rules
+ * of src/bvh.zig: leaf order spheres → mesh instances → meshes; random split
+ * axis per node, sort by aabb.min[axis], median split; children appended
+ * before the parent so each root is last; {inverse, forward} transform
+ * pairs per TLAS leaf; material and texture indices assigned in order of
+ * first use.  Matrices are zmath row-vector matrices (v' = v · M). */
+
+typedef struct orn_material_desc {
+    float albedo[3];
+    uint32_t texture;   /* index into orn_scene_desc.textures or ORN_NO_TEXTURE */
+    float fuzz;
+    float ior;
+    uint32_t type;      /* enum orn_material_type */
+} orn_material_desc;
+
+typedef struct orn_sphere_desc {       /* src/sphere.zig, src/scene.zig:124-134 */
+    float transform[16];
+    float aabb_min[3];
+    float aabb_max[3];
+    uint32_t material;
+} orn_sphere_desc;
+
+typedef struct orn_mesh_desc {         /* src/mesh.zig, src/scene.zig:263-316 */
+    const float* vertices;       uint32_t vertices_len;       /* 4 floats each */
+    const uint32_t* vertex_indices; uint32_t vertex_indices_len;
+    const float* normals;        uint32_t normals_len;        /* 4 floats each */
+    const uint32_t* normal_indices; uint32_t normal_indices_len;
+    const float* uvs;            uint32_t uvs_len;            /* 2 floats each */
+    const uint32_t* uv_indices;  uint32_t uv_indices_len;
+    float transform[16];
+    float aabb_min[3];
+    float aabb_max[3];
+    uint32_t material;
+} orn_mesh_desc;
+
+typedef struct orn_mesh_instance_desc { /* src/mesh_instance.zig */
+    uint32_t mesh;
+    float transform[16];
+    float aabb_min[3];
+    float aabb_max[3];
+    uint32_t material;
+} orn_mesh_instance_desc;
+
+typedef struct orn_scene_desc {
+    const orn_sphere_desc* spheres;               uint32_t spheres_len;
+    const orn_mesh_desc* meshes;                  uint32_t meshes_len;
+    const orn_mesh_instance_desc* mesh_instances; uint32_t mesh_instances_len;
+    const orn_material_desc* materials;           uint32_t materials_len;
+    const orn_texture* textures;                  uint32_t textures_len;
+    uint64_t seed;                /* split-axis PRNG seed (bvh.zig uses 1244) */
+    uint32_t row_major_transforms;/* 1 = HIP layout (transposed), 0 = wgpu   */
+} orn_scene_desc;
+
+typedef struct orn_bvh orn_bvh;
+
+/* Bvh.init — src/bvh.zig:33-78.  Returns ORN_ERR_EMPTY_SCENE for a scene
+ * without shapes or a mesh without triangles (the reference panics). */
+int orn_bvh_build(const orn_scene_desc* desc, orn_bvh** out);
+/* Fills `blob` with pointers into the builder's arrays (valid until
+ * orn_bvh_free).  Texture pointers refer to the caller's desc textures. */
+int orn_bvh_get_blob(const orn_bvh* bvh, orn_scene_blob* blob);
+/* Bvh.deinit — src/bvh.zig:80-90. */
+int orn_bvh_free(orn_bvh* bvh);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ORNAMENT_CUDA_H */

@@ -1,0 +1,264 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the reference
+(golden vectors recorded from its own HIP kernels) and the CPU oracle.
+
+Bit-exact throughout: hits, t values, node-visit counts, accumulation
+buffers, RNG states and framebuffers are compared as raw 32-bit words.  The
+kernels use the project's portable transcendentals, so images match the
+reference built with the same transcendentals ("pmath" fixtures) exactly."""
+import numpy as np
+import pytest
+
+from oracle import oracle_lib as ol
+from zig_ornament_gb300 import _lib, ornament, scenes
+
+pytestmark = pytest.mark.gpu
+
+W, H = 96, 64
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def make_state(depth=8, gamma=1.0, flip=False, iterations=1, semantics=_lib.SEMANTICS_HIP, spp_per_launch=0,
+               eps=0.001):
+    s = _lib.State()
+    s.depth, s.flip_y = depth, 1 if flip else 0
+    s.inverted_gamma = float(np.float32(1.0) / np.float32(gamma))
+    s.iterations, s.ray_cast_epsilon = iterations, eps
+    s.semantics, s.kernel, s.spp_per_launch = semantics, _lib.KERNEL_MEGA, spp_per_launch
+    return s
+
+
+@pytest.fixture(scope="module")
+def golden_renderer(golden_bvh):
+    r = ornament.Renderer(golden_bvh, device=0)
+    yield r
+    r.close()
+
+
+def test_trace_rays_matches_reference_and_oracle(golden, golden_bvh, golden_renderer, oracle):
+    golden_renderer.set_state(make_state())
+    hits, visits = golden_renderer.trace_rays(golden["rays"])
+    assert np.array_equal(bits(hits), bits(golden["ray_hits"]))       # reference's Bvh::hit
+    _, ovisits = oracle.trace_rays(golden_bvh, golden["rays"])
+    assert np.array_equal(visits, ovisits)                              # per-ray node visits
+
+
+def _golden_cases(golden):
+    for c in golden["render_cases"]:
+        name, spp, ci, depth, gamma, flip, base = str(c).split("|")
+        yield name, int(spp), float(ci), int(depth), float(gamma), bool(int(flip)), base or None
+
+
+def _flip_rows(fb, flip):
+    # the host build of the reference never flips (see tests/test_oracle_golden.py::reference_fb)
+    return fb.reshape(H, -1, 4)[::-1].reshape(-1, 4) if flip else fb
+
+
+def test_render_matches_reference_pmath(golden, golden_camera, golden_renderer):
+    """PathTracer.render semantics end to end: the fused single pass, a
+    multi-pass render, a continued (progressive) render, flip_y + gamma."""
+    r = golden_renderer
+    r.set_resolution(W, H)
+    states = {}
+    for name, spp, ci, depth, gamma, flip, base in _golden_cases(golden):
+        r.set_resolution(W, H)          # fresh target: RNG reseeded with the pixel index
+        r.set_state(make_state(depth=depth, gamma=gamma, flip=flip, iterations=spp))
+        r.set_camera(golden_camera)
+        if base:
+            acc0, rng0 = states[base]
+            r.set_progress(acc0, rng0, ci - 1.0)
+        r.render()
+        acc, rng, cur = r.progress()
+        fb = r.framebuffer()
+        states[name] = (acc, rng)
+        key = f"render_pmath_{name}"
+        assert cur == ci + spp - 1
+        assert np.array_equal(rng, golden[key + "_rng"]), name
+        assert np.array_equal(bits(acc), bits(golden[key + "_acc"])), name
+        assert np.array_equal(bits(fb), bits(_flip_rows(golden[key + "_fb"], flip))), name
+
+
+@pytest.mark.parametrize("spp_per_launch", [1, 2, 7])
+def test_launch_chunking_does_not_change_results(golden_camera, golden_renderer, golden, spp_per_launch):
+    r = golden_renderer
+    r.set_resolution(W, H)
+    r.set_state(make_state(gamma=2.2, iterations=5, spp_per_launch=spp_per_launch))
+    r.set_camera(golden_camera)
+    r.render()
+    acc, rng, _ = r.progress()
+    assert np.array_equal(bits(acc), bits(golden["render_pmath_pass5_acc"]))
+    assert np.array_equal(rng, golden["render_pmath_pass5_rng"])
+
+
+@pytest.mark.parametrize("semantics", [_lib.SEMANTICS_HIP, _lib.SEMANTICS_WGSL])
+def test_semantics_vs_oracle(golden_bvh, golden_camera, golden_renderer, oracle, semantics):
+    r = golden_renderer
+    r.set_resolution(W, H)
+    r.set_state(make_state(depth=10, gamma=2.2, iterations=4, semantics=semantics))
+    r.set_camera(golden_camera)
+    r.render()
+    acc, rng, _ = r.progress()
+    fb = r.framebuffer()
+    cp = ol.make_params(golden_camera, W, H, depth=10, gamma=2.2, textures_count=golden_bvh.scene_textures_count)
+    oacc, orng, ofb, _ = oracle.render(golden_bvh, cp, 4, semantics=semantics, portable_math=True)
+    assert np.array_equal(rng, orng)
+    assert np.array_equal(bits(acc), bits(oacc))
+    assert np.array_equal(bits(fb), bits(ofb))
+
+
+def test_camera_dirty_restarts_accumulation(golden_camera, golden_renderer, golden):
+    """update(): a dirty camera resets current_iteration
+    (src/hip_backend/path_tracer.zig:150-158); the RNG stream continues."""
+    r = golden_renderer
+    r.set_resolution(W, H)
+    r.set_state(make_state(gamma=2.2, iterations=5))
+    r.set_camera(golden_camera)
+    r.render()
+    _, rng5, _ = r.progress()
+    r.set_camera(golden_camera)           # same camera, but dirty
+    r.set_state(make_state(gamma=2.2, iterations=1))
+    r.render()
+    acc, rng, cur = r.progress()
+    assert cur == 1.0
+    assert (acc[:, 3] == 1.0).all()       # accumulation restarted
+    assert not np.array_equal(rng, rng5)  # the RNG stream moved on
+
+
+def test_set_resolution_reseeds(golden_camera, golden_renderer, golden):
+    r = golden_renderer
+    r.set_resolution(W, H)
+    r.set_state(make_state(gamma=2.2, iterations=5))
+    r.set_camera(golden_camera)
+    r.render()
+    r.set_resolution(W, H)
+    r.set_camera(golden_camera)
+    r.render()
+    acc, rng, _ = r.progress()
+    assert np.array_equal(rng, golden["render_pmath_pass5_rng"])
+
+
+def test_errors_are_statuses(golden_bvh, golden_renderer):
+    r = golden_renderer
+    r.set_resolution(W, H)
+    with pytest.raises(_lib.OrnamentError) as e:
+        r._check(r._lib.orn_get_framebuffer(r.handle, np.zeros(16, np.float32).ctypes.data, 4))
+    assert e.value.status == 8
+    fresh = ornament.Renderer(golden_bvh, device=0)
+    with pytest.raises(_lib.OrnamentError) as e:
+        fresh.render()                     # no camera yet
+    assert e.value.status == 1
+    fresh.close()
+    bad = ornament.Bvh.from_arrays(**{k: getattr(golden_bvh, k) for k in
+                                     ("blas_nodes", "normals", "normal_indices", "uvs", "uv_indices",
+                                      "transforms", "materials", "textures", "scene_textures_count")},
+                                   tlas_nodes=golden_bvh.tlas_nodes.copy())
+    bad.tlas_nodes["left_or_custom_id"][-1] = len(bad.tlas_nodes) + 5
+    with pytest.raises(_lib.OrnamentError) as e:
+        ornament.Renderer(bad, device=0)
+    assert e.value.status == 6
+
+
+def test_pathtracer_surface_end_to_end(oracle):
+    """The ornament.zig-style driver loop: State setters, setResolution,
+    render, getFrameBuffer, camera move (setLookAt)."""
+    scene = scenes.small_test_scene(64, 40, seed=9)
+    pt = ornament.PathTracer(scene, device=0)
+    pt.state.setGamma(2.2)
+    pt.state.setFlipY(True)
+    pt.state.setDepth(6)
+    pt.state.setIterations(3)
+    pt.setResolution(ornament.Resolution(64, 40))
+    pt.render()
+    fb1 = pt.getFrameBuffer().copy()
+    cp = ol.make_params(scene.camera, 64, 40, depth=6, gamma=2.2, flip_y=True,
+                        textures_count=pt.bvh.scene_textures_count)
+    _, _, ofb, _ = oracle.render(pt.bvh, cp, 3)
+    assert np.array_equal(bits(fb1), bits(ofb))
+    scene.camera.setLookAt(ornament.f32x4(1, 3, 12, 1), ornament.f32x4(0, 0.5, 0, 1), ornament.f32x4(0, 1, 0, 0))
+    pt.render()
+    fb2 = pt.getFrameBuffer()
+    assert not np.array_equal(fb1, fb2)
+    _, _, ci = pt.getProgress()
+    assert ci == 3.0
+    pt.deinit()
+
+
+def test_sphere_field_and_instanced_vs_oracle(oracle):
+    for scene, w, h, depth in ((scenes.spheres_scene(80, 45, seed=0), 80, 45, 10),
+                               (scenes.instanced_meshes_scene(96, 54, seed=1, n_blas=4, n_instances=40,
+                                                              tri_range=(2000, 8000), texture_size=128), 96, 54, 8)):
+        bvh = ornament.Bvh(scene)
+        r = ornament.Renderer(bvh, device=0)
+        r.set_resolution(w, h)
+        r.set_state(make_state(depth=depth, gamma=2.2, iterations=2))
+        r.set_camera(scene.camera.to_struct())
+        r.render()
+        acc, rng, _ = r.progress()
+        cp = ol.make_params(scene.camera, w, h, depth=depth, gamma=2.2, textures_count=bvh.scene_textures_count)
+        oacc, orng, _, _ = oracle.render(bvh, cp, 2)
+        assert np.array_equal(rng, orng)
+        assert np.array_equal(bits(acc), bits(oacc))
+        r.close()
+
+
+def _primary_rays(cam, w, h, n, rs):
+    """Camera rays (camera.hip.h:25-33 formula, float32) at random pixels."""
+    px = rs.integers(0, w, n)
+    py = rs.integers(0, h, n)
+    u = ((px + rs.random(n)) / (w - 1)).astype(np.float32)[:, None]
+    v = ((py + rs.random(n)) / (h - 1)).astype(np.float32)[:, None]
+    o = np.array(cam.origin[:], np.float32)
+    d = (np.array(cam.lower_left_corner[:], np.float32) + u * np.array(cam.horizontal[:], np.float32)
+         + v * np.array(cam.vertical[:], np.float32) - o)
+    return np.concatenate([np.broadcast_to(o, d.shape), d], 1).astype(np.float32)
+
+
+def test_primary_hits_instanced_1080p_scene(oracle):
+    """The benchmark scene (8 BLAS, 256 instances, 281k triangles): primary
+    hit instance/primitive ids, t and node-visit counts, bit-exact."""
+    scene = scenes.instanced_meshes_scene()
+    bvh = ornament.Bvh(scene)
+    r = ornament.Renderer(bvh, device=0)
+    r.set_state(make_state())
+    rays = _primary_rays(scene.camera.to_struct(), 1920, 1080, 200_000, np.random.default_rng(5))
+    hits, visits = r.trace_rays(rays)
+    ohits, ovisits = oracle.trace_rays(bvh, rays)
+    assert np.array_equal(bits(hits), bits(ohits))
+    assert np.array_equal(visits, ovisits)
+    assert hits["hit"].mean() > 0.05
+    r.close()
+
+
+@pytest.mark.slow
+def test_full_size_properties_1080p():
+    """Full-size (1920x1080) properties: deterministic, progressive renders
+    equal one-shot renders, alpha counts the samples, values finite, work
+    counters consistent."""
+    scene = scenes.instanced_meshes_scene()
+    bvh = ornament.Bvh(scene)
+    a = ornament.Renderer(bvh, device=0)
+    b = ornament.Renderer(bvh, device=0)
+    for r in (a, b):
+        r.set_resolution(1920, 1080)
+        r.set_camera(scene.camera.to_struct())
+    a.set_state(make_state(iterations=4))
+    a.enable_counters(True)
+    a.render()
+    b.set_state(make_state(iterations=2))
+    b.render()
+    b.render()
+    acc_a, rng_a, ci_a = a.progress()
+    acc_b, rng_b, ci_b = b.progress()
+    assert ci_a == ci_b == 4.0
+    assert np.array_equal(bits(acc_a), bits(acc_b)) and np.array_equal(rng_a, rng_b)
+    assert (acc_a[:, 3] == 4.0).all()
+    assert np.isfinite(acc_a).all()
+    c = a.counters()
+    assert c["samples"] == 4 * 1920 * 1080
+    assert c["rays"] >= c["samples"]
+    assert c["visits"] == c["internal"] + c["sphere_leaf"] + c["mesh_entry"] + c["triangle"]
+    assert c["sphere_hits"] + c["mesh_hits"] <= c["rays"]
+    a.close()
+    b.close()

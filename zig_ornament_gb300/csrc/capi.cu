@@ -1,0 +1,609 @@
+// capi.cu — host side of libornament_cuda: the C ABI declared in
+// include/ornament_cuda.h.
+//
+// A context mirrors the HIP backend's PathTracer
+// (src/hip_backend/path_tracer.zig:12-236): it owns the device copy of the
+// scene arrays, the lazily created target buffers (framebuffer,
+// accumulation, per-pixel RNG state), the State fields and the camera with
+// its dirty flag.  render() follows PathTracer.render/update (:121-168):
+// a dirty camera resets current_iteration, each of the `iterations` passes
+// advances it by one, and post-processing uses the last value.  The passes
+// are issued as one or more megakernel launches on the context's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ornament_cuda.h"
+#include "pt_kernels.h"
+
+using orn::RenderLaunch;
+using orn::SceneDev;
+using orn::TexDesc;
+
+struct orn_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    std::vector<void*> scene_allocs;
+    SceneDev scene{};
+    uint32_t scene_textures_count = 0;
+    uint32_t tlas_len = 0, blas_len = 0;
+
+    orn_state state{};
+    orn_camera camera{};
+    bool camera_set = false;
+    bool camera_dirty = true;
+    float current_iteration = 0.0f;
+
+    uint32_t width = 500, height = 500;   // State.init resolution
+    bool target_valid = false;
+    float4* acc = nullptr;
+    float4* fb = nullptr;
+    uint32_t* rng = nullptr;
+
+    uint32_t* d_error = nullptr;
+    unsigned long long* d_counters = nullptr;
+    bool counters_enabled = false;
+    bool rendered = false;
+    uint64_t launches = 0;
+    std::string last_error;
+};
+
+namespace {
+
+int fail(orn_context* ctx, int status, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return status;
+}
+
+int cuda_fail(orn_context* ctx, cudaError_t e, const char* what) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return fail(ctx, ORN_ERR_OUT_OF_MEMORY, msg);
+    if (e == cudaErrorNoDevice || e == cudaErrorInvalidDevice || e == cudaErrorInsufficientDriver)
+        return fail(ctx, ORN_ERR_NO_DEVICE, msg);
+    return fail(ctx, ORN_ERR_CUDA, msg);
+}
+
+#define ORN_CUDA(ctx, call)                                         \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call);  \
+    } while (0)
+
+orn_state default_state() {
+    orn_state s;
+    std::memset(&s, 0, sizeof(s));
+    s.depth = 10;
+    s.flip_y = 0;
+    s.inverted_gamma = 1.0f;
+    s.iterations = 1;
+    s.ray_cast_epsilon = 0.001f;
+    s.semantics = ORN_SEMANTICS_HIP;
+    s.kernel = ORN_KERNEL_MEGA;
+    s.spp_per_launch = 0;
+    return s;
+}
+
+// Blob validation: every index the kernels follow must be in range, and
+// internal nodes must point at lower ids (children are appended before
+// their parent in src/bvh.zig), which rules out cycles.
+int validate_blob(orn_context* ctx, const orn_scene_blob* b) {
+    if (!b) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "blob is NULL");
+    if (b->tlas_nodes_len == 0 || !b->tlas_nodes)
+        return fail(ctx, ORN_ERR_EMPTY_SCENE, "scene cannot be empty (no TLAS nodes)");
+    if ((b->blas_nodes_len && !b->blas_nodes) || (b->normals_len && !b->normals) ||
+        (b->normal_indices_len && !b->normal_indices) || (b->uvs_len && !b->uvs) ||
+        (b->uv_indices_len && !b->uv_indices) || (b->transforms_len && !b->transforms) ||
+        (b->materials_len && !b->materials) || (b->textures_len && !b->textures))
+        return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "blob array pointer is NULL with nonzero length");
+    if ((uint64_t)b->tlas_nodes_len + b->blas_nodes_len >= 0xFFFFFFFFull)
+        return fail(ctx, ORN_ERR_BAD_SCENE, "too many nodes");
+    for (uint32_t i = 0; i < b->tlas_nodes_len; ++i) {
+        const orn_bvh_node& n = b->tlas_nodes[i];
+        switch (n.node_type) {
+            case ORN_NODE_INTERNAL:
+                if (n.left_or_custom_id >= i || n.right_or_material_index >= i)
+                    return fail(ctx, ORN_ERR_BAD_SCENE, "TLAS internal node child out of range");
+                break;
+            case ORN_NODE_SPHERE:
+            case ORN_NODE_MESH:
+                if ((uint64_t)n.transform_id * 2 + 1 >= b->transforms_len)
+                    return fail(ctx, ORN_ERR_BAD_SCENE, "TLAS leaf transform_id out of range");
+                if (n.right_or_material_index >= b->materials_len)
+                    return fail(ctx, ORN_ERR_BAD_SCENE, "TLAS leaf material out of range");
+                if (n.node_type == ORN_NODE_MESH && n.left_or_custom_id >= b->blas_nodes_len)
+                    return fail(ctx, ORN_ERR_BAD_SCENE, "mesh leaf BLAS root out of range");
+                break;
+            default:
+                return fail(ctx, ORN_ERR_BAD_SCENE, "invalid TLAS node type");
+        }
+    }
+    for (uint32_t i = 0; i < b->blas_nodes_len; ++i) {
+        const orn_bvh_node& n = b->blas_nodes[i];
+        if (n.node_type == ORN_NODE_INTERNAL) {
+            if (n.left_or_custom_id >= i || n.right_or_material_index >= i)
+                return fail(ctx, ORN_ERR_BAD_SCENE, "BLAS internal node child out of range");
+        } else if (n.node_type == ORN_NODE_TRIANGLE) {
+            uint64_t last = (uint64_t)n.left_or_custom_id * 3 + 2;
+            if (last >= b->normal_indices_len || last >= b->uv_indices_len)
+                return fail(ctx, ORN_ERR_BAD_SCENE, "triangle id out of range of the index arrays");
+        } else {
+            return fail(ctx, ORN_ERR_BAD_SCENE, "invalid BLAS node type");
+        }
+    }
+    for (uint32_t i = 0; i < b->normal_indices_len; ++i)
+        if (b->normal_indices[i] >= b->normals_len)
+            return fail(ctx, ORN_ERR_BAD_SCENE, "normal index out of range");
+    for (uint32_t i = 0; i < b->uv_indices_len; ++i)
+        if (b->uv_indices[i] >= b->uvs_len) return fail(ctx, ORN_ERR_BAD_SCENE, "uv index out of range");
+    for (uint32_t i = 0; i < b->textures_len; ++i) {
+        const orn_texture& t = b->textures[i];
+        uint32_t texel = t.format == ORN_TEXEL_RGBA8 ? 4u : 8u;
+        if (!t.data || t.width == 0 || t.height == 0 || t.format > ORN_TEXEL_RGBA16F ||
+            t.bytes_per_row < t.width * texel)
+            return fail(ctx, ORN_ERR_BAD_SCENE, "invalid texture");
+    }
+    return ORN_OK;
+}
+
+template <typename T>
+int upload(orn_context* ctx, const T* host, size_t count, T** dev) {
+    *dev = nullptr;
+    size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    void* p = nullptr;
+    ORN_CUDA(ctx, cudaMalloc(&p, bytes));
+    ctx->scene_allocs.push_back(p);
+    if (count) ORN_CUDA(ctx, cudaMemcpy(p, host, count * sizeof(T), cudaMemcpyHostToDevice));
+    *dev = (T*)p;
+    return ORN_OK;
+}
+
+// Re-lays the reference's BvhNode arrays into the kernel's node array.
+void relayout_nodes(const orn_scene_blob* b, std::vector<float4>* out) {
+    const uint32_t T = b->tlas_nodes_len, B = b->blas_nodes_len;
+    out->assign((size_t)(T + B) * 4, make_float4(0, 0, 0, 0));
+    auto u2f = [](uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; };
+    auto put = [&](size_t idx, const orn_bvh_node& n, uint32_t child_offset) {
+        float4* o = out->data() + idx * 4;
+        const float* a = n.left_aabb_min_or_v0;
+        const float* bb = n.left_aabb_max_or_v1;
+        const float* c = n.right_aabb_min_or_v2;
+        const float* e = n.right_aabb_max_or_v3;
+        switch (n.node_type) {
+            case ORN_NODE_INTERNAL:
+                o[0] = make_float4(a[0], a[1], a[2], u2f(n.left_or_custom_id + child_offset));
+                o[1] = make_float4(bb[0], bb[1], bb[2], u2f(n.right_or_material_index + child_offset));
+                o[2] = make_float4(c[0], c[1], c[2], u2f(ORN_NODE_INTERNAL));
+                o[3] = make_float4(e[0], e[1], e[2], 0.0f);
+                break;
+            case ORN_NODE_TRIANGLE:
+                // e1 = v1 - v0, e2 = v2 - v0: the subtractions of bvh.hip.h:81-82
+                o[0] = make_float4(a[0], a[1], a[2], u2f(n.left_or_custom_id));
+                o[1] = make_float4(bb[0] - a[0], bb[1] - a[1], bb[2] - a[2], 0.0f);
+                o[2] = make_float4(c[0] - a[0], c[1] - a[1], c[2] - a[2], u2f(ORN_NODE_TRIANGLE));
+                o[3] = make_float4(0, 0, 0, 0);
+                break;
+            default: {  // sphere / mesh leaf: inverse rows 0..2 inline
+                const float* m = b->transforms + (size_t)n.transform_id * 2 * 16;
+                o[0] = make_float4(m[0], m[1], m[2], m[3]);
+                o[1] = make_float4(m[4], m[5], m[6], m[7]);
+                o[2] = make_float4(m[8], m[9], m[10], u2f(n.node_type));
+                uint32_t root = n.node_type == ORN_NODE_MESH ? n.left_or_custom_id + T : 0u;
+                o[3] = make_float4(m[11], u2f(n.right_or_material_index), u2f(n.transform_id), u2f(root));
+                break;
+            }
+        }
+    };
+    for (uint32_t i = 0; i < T; ++i) put(i, b->tlas_nodes[i], 0);
+    for (uint32_t i = 0; i < B; ++i) put((size_t)T + i, b->blas_nodes[i], T);
+}
+
+int ensure_target(orn_context* ctx) {
+    if (ctx->target_valid) return ORN_OK;
+    size_t n = (size_t)ctx->width * ctx->height;
+    if (n == 0) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "resolution is zero");
+    if (n >= 0xFFFFFFFFull) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "resolution too large");
+    ORN_CUDA(ctx, cudaMalloc(&ctx->acc, n * sizeof(float4)));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->fb, n * sizeof(float4)));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->rng, n * sizeof(uint32_t)));
+    ORN_CUDA(ctx, cudaMemsetAsync(ctx->acc, 0, n * sizeof(float4), ctx->stream));
+    ORN_CUDA(ctx, cudaMemsetAsync(ctx->fb, 0, n * sizeof(float4), ctx->stream));
+    ORN_CUDA(ctx, orn::launch_seed_rng(ctx->rng, (uint32_t)n, ctx->stream));
+    ctx->target_valid = true;
+    return ORN_OK;
+}
+
+void free_target(orn_context* ctx) {
+    if (ctx->acc) cudaFree(ctx->acc);
+    if (ctx->fb) cudaFree(ctx->fb);
+    if (ctx->rng) cudaFree(ctx->rng);
+    ctx->acc = nullptr;
+    ctx->fb = nullptr;
+    ctx->rng = nullptr;
+    ctx->target_valid = false;
+}
+
+// Synchronises and turns the device error word into a status.
+int sync_and_check(orn_context* ctx) {
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    ORN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t err = 0;
+    ORN_CUDA(ctx, cudaMemcpy(&err, ctx->d_error, 4, cudaMemcpyDeviceToHost));
+    if (err) {
+        ORN_CUDA(ctx, cudaMemset(ctx->d_error, 0, 4));
+        if (err & orn::ERR_STACK)
+            return fail(ctx, ORN_ERR_STACK_OVERFLOW, "a ray needed more than 64 traversal stack entries");
+        return fail(ctx, ORN_ERR_TIMEOUT, "a ray exceeded the per-ray node-visit limit");
+    }
+    return ORN_OK;
+}
+
+orn_constant_params make_params(const orn_context* ctx, float current_iteration) {
+    orn_constant_params cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.camera = ctx->camera;
+    cp.depth = ctx->state.depth;
+    cp.width = ctx->width;
+    cp.height = ctx->height;
+    cp.flip_y = ctx->state.flip_y ? 1u : 0u;
+    cp.inverted_gamma = ctx->state.inverted_gamma;
+    cp.ray_cast_epsilon = ctx->state.ray_cast_epsilon;
+    cp.textures_count = ctx->scene_textures_count;
+    cp.current_iteration = current_iteration;
+    return cp;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t orn_abi_version(void) { return ORN_ABI_VERSION; }
+
+const char* orn_status_string(int status) {
+    switch (status) {
+        case ORN_OK: return "ok";
+        case ORN_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case ORN_ERR_EMPTY_SCENE: return "empty scene";
+        case ORN_ERR_OUT_OF_MEMORY: return "out of memory";
+        case ORN_ERR_CUDA: return "CUDA error";
+        case ORN_ERR_NO_DEVICE: return "no CUDA device";
+        case ORN_ERR_BAD_SCENE: return "invalid scene data";
+        case ORN_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+        case ORN_ERR_BUFFER_TOO_SMALL: return "buffer too small";
+        case ORN_ERR_TIMEOUT: return "device-side limit reached";
+        default: return "unknown status";
+    }
+}
+
+const char* orn_last_error(const orn_context* ctx) {
+    return ctx ? ctx->last_error.c_str() : "context is NULL";
+}
+
+int orn_create(const orn_scene_blob* blob, int device, orn_context** out) {
+    if (!out) return ORN_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int st = validate_blob(nullptr, blob);
+    if (st != ORN_OK) return st;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return ORN_ERR_NO_DEVICE;
+    if (device < 0) device = count - 1;
+    if (device >= count) return ORN_ERR_NO_DEVICE;
+    orn_context* ctx = new (std::nothrow) orn_context();
+    if (!ctx) return ORN_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    ctx->state = default_state();
+    st = [&]() -> int {
+        ORN_CUDA(ctx, cudaSetDevice(device));
+        ORN_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ORN_CUDA(ctx, cudaEventCreate(&ctx->ev_start));
+        ORN_CUDA(ctx, cudaEventCreate(&ctx->ev_stop));
+        ORN_CUDA(ctx, cudaMalloc(&ctx->d_error, 4));
+        ORN_CUDA(ctx, cudaMemset(ctx->d_error, 0, 4));
+        ORN_CUDA(ctx, cudaMalloc(&ctx->d_counters, ORN_COUNTER_COUNT * sizeof(unsigned long long)));
+        ORN_CUDA(ctx, cudaMemset(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long)));
+        std::vector<float4> nodes;
+        relayout_nodes(blob, &nodes);
+        float4* d_nodes = nullptr;
+        int s = upload(ctx, nodes.data(), nodes.size(), &d_nodes);
+        if (s) return s;
+        float4* d_x = nullptr;
+        if ((s = upload(ctx, (const float4*)blob->transforms, (size_t)blob->transforms_len * 4, &d_x))) return s;
+        float4* d_n = nullptr;
+        if ((s = upload(ctx, (const float4*)blob->normals, (size_t)blob->normals_len, &d_n))) return s;
+        uint32_t* d_ni = nullptr;
+        if ((s = upload(ctx, blob->normal_indices, blob->normal_indices_len, &d_ni))) return s;
+        float2* d_uv = nullptr;
+        if ((s = upload(ctx, (const float2*)blob->uvs, (size_t)blob->uvs_len, &d_uv))) return s;
+        uint32_t* d_ui = nullptr;
+        if ((s = upload(ctx, blob->uv_indices, blob->uv_indices_len, &d_ui))) return s;
+        float4* d_m = nullptr;
+        if ((s = upload(ctx, (const float4*)blob->materials, (size_t)blob->materials_len * 2, &d_m))) return s;
+        // Textures: one device copy per distinct host image (the builder
+        // appends a texture once per material that uses it).
+        std::map<std::pair<const void*, uint64_t>, const unsigned char*> seen;
+        std::vector<TexDesc> descs(blob->textures_len);
+        for (uint32_t i = 0; i < blob->textures_len; ++i) {
+            const orn_texture& t = blob->textures[i];
+            uint32_t texel = t.format == ORN_TEXEL_RGBA8 ? 4u : 8u;
+            uint32_t pitch = t.width * texel;
+            auto key = std::make_pair(t.data, ((uint64_t)t.width << 32) | t.height);
+            const unsigned char* dptr = nullptr;
+            auto it = seen.find(key);
+            if (it != seen.end()) {
+                dptr = it->second;
+            } else {
+                void* p = nullptr;
+                ORN_CUDA(ctx, cudaMalloc(&p, (size_t)pitch * t.height));
+                ctx->scene_allocs.push_back(p);
+                ORN_CUDA(ctx, cudaMemcpy2D(p, pitch, t.data, t.bytes_per_row, pitch, t.height,
+                                           cudaMemcpyHostToDevice));
+                dptr = (const unsigned char*)p;
+                seen[key] = dptr;
+            }
+            descs[i] = TexDesc{dptr, t.width, t.height, pitch, t.format};
+        }
+        TexDesc* d_t = nullptr;
+        if ((s = upload(ctx, descs.data(), descs.size(), &d_t))) return s;
+        ctx->scene.nodes = d_nodes;
+        ctx->scene.tlas_len = blob->tlas_nodes_len;
+        ctx->scene.node_count = blob->tlas_nodes_len + blob->blas_nodes_len;
+        ctx->scene.xforms = d_x;
+        ctx->scene.normals = d_n;
+        ctx->scene.normal_indices = d_ni;
+        ctx->scene.uvs = d_uv;
+        ctx->scene.uv_indices = d_ui;
+        ctx->scene.materials = d_m;
+        ctx->scene.textures = d_t;
+        ctx->scene.textures_len = blob->textures_len;
+        ctx->scene_textures_count = blob->scene_textures_count;
+        ctx->tlas_len = blob->tlas_nodes_len;
+        ctx->blas_len = blob->blas_nodes_len;
+        return ORN_OK;
+    }();
+    if (st != ORN_OK) {
+        orn_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return ORN_OK;
+}
+
+int orn_destroy(orn_context* ctx) {
+    if (!ctx) return ORN_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_target(ctx);
+    for (void* p : ctx->scene_allocs) cudaFree(p);
+    if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+    if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return ORN_OK;
+}
+
+int orn_set_state(orn_context* ctx, const orn_state* s) {
+    if (!ctx || !s) return ORN_ERR_INVALID_ARGUMENT;
+    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_WAVEFRONT)
+        return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics or kernel");
+    ctx->state = *s;
+    return ORN_OK;
+}
+
+int orn_get_state(const orn_context* ctx, orn_state* out) {
+    if (!ctx || !out) return ORN_ERR_INVALID_ARGUMENT;
+    *out = ctx->state;
+    return ORN_OK;
+}
+
+int orn_set_camera(orn_context* ctx, const orn_camera* camera) {
+    if (!ctx || !camera) return ORN_ERR_INVALID_ARGUMENT;
+    ctx->camera = *camera;
+    ctx->camera_set = true;
+    ctx->camera_dirty = true;
+    return ORN_OK;
+}
+
+int orn_set_resolution(orn_context* ctx, uint32_t width, uint32_t height) {
+    if (!ctx || width == 0 || height == 0) return ORN_ERR_INVALID_ARGUMENT;
+    if ((uint64_t)width * height >= 0xFFFFFFFFull)
+        return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "resolution too large");
+    cudaSetDevice(ctx->device);
+    if (ctx->target_valid) {
+        cudaStreamSynchronize(ctx->stream);
+        free_target(ctx);
+    }
+    ctx->width = width;
+    ctx->height = height;
+    return ORN_OK;
+}
+
+int orn_get_resolution(const orn_context* ctx, uint32_t* w, uint32_t* h) {
+    if (!ctx || !w || !h) return ORN_ERR_INVALID_ARGUMENT;
+    *w = ctx->width;
+    *h = ctx->height;
+    return ORN_OK;
+}
+
+int orn_peek_constant_params(const orn_context* ctx, orn_constant_params* out) {
+    if (!ctx || !out) return ORN_ERR_INVALID_ARGUMENT;
+    float ci = ctx->camera_dirty ? 0.0f : ctx->current_iteration;
+    *out = make_params(ctx, ci + 1.0f);
+    return ORN_OK;
+}
+
+int orn_render(orn_context* ctx) {
+    if (!ctx) return ORN_ERR_INVALID_ARGUMENT;
+    if (!ctx->camera_set) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "no camera set (orn_set_camera)");
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_target(ctx);
+    if (st) return st;
+    if (ctx->camera_dirty) {
+        ctx->current_iteration = 0.0f;
+        ctx->camera_dirty = false;
+    }
+    // iterations <= 1 takes the fused path of the reference: one pass.
+    const uint32_t passes = std::max<uint32_t>(ctx->state.iterations, 1u);
+    const float ci_start = ctx->current_iteration + 1.0f;
+    ctx->current_iteration += (float)passes;
+    uint32_t chunk = ctx->state.spp_per_launch;
+    if (chunk == 0) chunk = passes <= 64 ? passes : 32;
+    RenderLaunch p;
+    std::memset(&p, 0, sizeof(p));
+    p.scene = ctx->scene;
+    p.pixel_count = ctx->width * ctx->height;
+    p.acc = ctx->acc;
+    p.fb = ctx->fb;
+    p.rng = ctx->rng;
+    p.error = ctx->d_error;
+    p.counters = ctx->d_counters;
+    if (ctx->counters_enabled)
+        ORN_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long), ctx->stream));
+    ORN_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    for (uint32_t done = 0; done < passes;) {
+        uint32_t n = std::min(chunk, passes - done);
+        p.cp = make_params(ctx, ci_start + (float)done);
+        p.spp = n;
+        p.do_post = (done + n == passes) ? 1u : 0u;
+        ORN_CUDA(ctx, orn::launch_mega(p, (int)ctx->state.semantics, orn::MATH_PORTABLE,
+                                       ctx->counters_enabled, ctx->stream));
+        ctx->launches++;
+        done += n;
+    }
+    ORN_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    ctx->rendered = true;
+    return ORN_OK;
+}
+
+int orn_synchronize(orn_context* ctx) {
+    if (!ctx) return ORN_ERR_INVALID_ARGUMENT;
+    return sync_and_check(ctx);
+}
+
+int orn_last_render_ms(orn_context* ctx, float* ms) {
+    if (!ctx || !ms) return ORN_ERR_INVALID_ARGUMENT;
+    if (!ctx->rendered) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "nothing rendered yet");
+    int st = sync_and_check(ctx);
+    if (st) return st;
+    ORN_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev_start, ctx->ev_stop));
+    return ORN_OK;
+}
+
+int orn_get_framebuffer(orn_context* ctx, float* dst, size_t pixel_count) {
+    if (!ctx || !dst) return ORN_ERR_INVALID_ARGUMENT;
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_target(ctx);
+    if (st) return st;
+    size_t n = (size_t)ctx->width * ctx->height;
+    if (pixel_count < n) return fail(ctx, ORN_ERR_BUFFER_TOO_SMALL, "framebuffer destination too small");
+    ORN_CUDA(ctx, cudaMemcpyAsync(dst, ctx->fb, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+int orn_get_accumulation(orn_context* ctx, float* dst, size_t pixel_count) {
+    if (!ctx || !dst) return ORN_ERR_INVALID_ARGUMENT;
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_target(ctx);
+    if (st) return st;
+    size_t n = (size_t)ctx->width * ctx->height;
+    if (pixel_count < n) return fail(ctx, ORN_ERR_BUFFER_TOO_SMALL, "accumulation destination too small");
+    ORN_CUDA(ctx, cudaMemcpyAsync(dst, ctx->acc, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+int orn_get_progress(orn_context* ctx, float* accumulation, uint32_t* rng_state, size_t pixel_count,
+                     float* current_iteration) {
+    if (!ctx || !accumulation || !rng_state || !current_iteration) return ORN_ERR_INVALID_ARGUMENT;
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_target(ctx);
+    if (st) return st;
+    size_t n = (size_t)ctx->width * ctx->height;
+    if (pixel_count < n) return fail(ctx, ORN_ERR_BUFFER_TOO_SMALL, "progress destination too small");
+    ORN_CUDA(ctx, cudaMemcpyAsync(accumulation, ctx->acc, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    ORN_CUDA(ctx, cudaMemcpyAsync(rng_state, ctx->rng, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    st = sync_and_check(ctx);
+    if (st) return st;
+    *current_iteration = ctx->camera_dirty ? 0.0f : ctx->current_iteration;
+    return ORN_OK;
+}
+
+int orn_set_progress(orn_context* ctx, const float* accumulation, const uint32_t* rng_state,
+                     size_t pixel_count, float current_iteration) {
+    if (!ctx || !accumulation || !rng_state || current_iteration < 0.0f) return ORN_ERR_INVALID_ARGUMENT;
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_target(ctx);
+    if (st) return st;
+    size_t n = (size_t)ctx->width * ctx->height;
+    if (pixel_count != n) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "progress size does not match the resolution");
+    ORN_CUDA(ctx, cudaMemcpyAsync(ctx->acc, accumulation, n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    ORN_CUDA(ctx, cudaMemcpyAsync(ctx->rng, rng_state, n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+    st = sync_and_check(ctx);
+    if (st) return st;
+    ctx->current_iteration = current_iteration;
+    ctx->camera_dirty = false;
+    return ORN_OK;
+}
+
+int orn_trace_rays(orn_context* ctx, const orn_ray* rays, size_t count, orn_hit* hits, uint32_t* visits) {
+    if (!ctx || (count && (!rays || !hits))) return ORN_ERR_INVALID_ARGUMENT;
+    if (count == 0) return ORN_OK;
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    float* d_rays = nullptr;
+    orn_hit* d_hits = nullptr;
+    uint32_t* d_visits = nullptr;
+    int st = [&]() -> int {
+        ORN_CUDA(ctx, cudaMalloc(&d_rays, count * sizeof(orn_ray)));
+        ORN_CUDA(ctx, cudaMalloc(&d_hits, count * sizeof(orn_hit)));
+        if (visits) ORN_CUDA(ctx, cudaMalloc(&d_visits, count * sizeof(uint32_t)));
+        ORN_CUDA(ctx, cudaMemcpyAsync(d_rays, rays, count * sizeof(orn_ray), cudaMemcpyHostToDevice, ctx->stream));
+        ORN_CUDA(ctx, orn::launch_trace_rays(ctx->scene, ctx->state.ray_cast_epsilon, d_rays, count, d_hits,
+                                             d_visits, ctx->d_error, ctx->stream));
+        ORN_CUDA(ctx, cudaMemcpyAsync(hits, d_hits, count * sizeof(orn_hit), cudaMemcpyDeviceToHost, ctx->stream));
+        if (visits)
+            ORN_CUDA(ctx, cudaMemcpyAsync(visits, d_visits, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        return sync_and_check(ctx);
+    }();
+    cudaStreamSynchronize(ctx->stream);
+    if (d_rays) cudaFree(d_rays);
+    if (d_hits) cudaFree(d_hits);
+    if (d_visits) cudaFree(d_visits);
+    return st;
+}
+
+int orn_get_stream(const orn_context* ctx, void** stream) {
+    if (!ctx || !stream) return ORN_ERR_INVALID_ARGUMENT;
+    *stream = (void*)ctx->stream;
+    return ORN_OK;
+}
+
+int orn_launch_count(const orn_context* ctx, uint64_t* launches) {
+    if (!ctx || !launches) return ORN_ERR_INVALID_ARGUMENT;
+    *launches = ctx->launches;
+    return ORN_OK;
+}
+
+int orn_enable_counters(orn_context* ctx, int enable) {
+    if (!ctx) return ORN_ERR_INVALID_ARGUMENT;
+    ctx->counters_enabled = enable != 0;
+    return ORN_OK;
+}
+
+int orn_get_counters(orn_context* ctx, uint64_t* out, size_t count) {
+    if (!ctx || !out) return ORN_ERR_INVALID_ARGUMENT;
+    int st = sync_and_check(ctx);
+    if (st) return st;
+    unsigned long long tmp[ORN_COUNTER_COUNT];
+    ORN_CUDA(ctx, cudaMemcpy(tmp, ctx->d_counters, sizeof(tmp), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < count && i < ORN_COUNTER_COUNT; ++i) out[i] = tmp[i];
+    return ORN_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,440 @@
+// pt_device.cuh — device-side core of the sm_103a path tracer.
+//
+// What it computes is zig_ornament's per-pixel path-tracing hot path
+// (src/hip_backend/kernels/pathtracer.hip.cpp:72-154 and the headers it
+// includes; the WGSL twins under src/wgpu_backend/shaders/ compute the same
+// formulas).  How it computes it is GB300-specific:
+//
+//  * One node array for TLAS and BLAS (BLAS ids offset by the TLAS length),
+//    64-byte nodes fetched as four 16-byte read-only vector loads
+//    (ld.global.nc.v4).  Sphere and mesh-entry leaves carry rows 0-2 of
+//    their inverse transform inline, so a leaf visit is one node fetch
+//    instead of node + transform; triangle leaves carry v0 and the two
+//    precomputed edges (the same float subtractions the reference does).
+//  * The reference's explicit stack loop (bvh.hip.h:145-276: push left,
+//    push right, pop; a 0xffffffff sentinel marks the BLAS exit) is run as
+//    "keep the next node in a register, push only the deferred child" with
+//    the BLAS exit detected by stack depth.  Nodes are visited in exactly
+//    the reference's order, so hits and per-ray visit counts are identical.
+//  * All arithmetic keeps the reference's operation order; the translation
+//    unit is compiled with -fmad=false so no multiply-add is contracted.
+//    With MATH_PORTABLE the transcendentals come from pmath.h and every
+//    sample is bit-identical to the CPU restatement.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ornament_cuda.h"
+#include "pmath.h"
+#include "pt_scene.h"
+
+namespace orn {
+
+constexpr uint32_t kMaxVisitsPerRay = 1u << 24;
+constexpr int kStackSize = 64;
+
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 add(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 sub(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 mul(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 scale(float c, f3 a) { return {c * a.x, c * a.y, c * a.z}; }
+__device__ __forceinline__ f3 neg(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ f3 normalize(f3 a) {
+    float l = sqrtf(dot(a, a));
+    return {a.x / l, a.y / l, a.z / l};
+}
+__device__ __forceinline__ f3 reflect(f3 e1, f3 e2) { return sub(e1, scale(2.0f * dot(e2, e1), e2)); }
+__device__ __forceinline__ f3 refract(f3 i, f3 n, float eta) {
+    float k = 1.0f - eta * eta * (1.0f - dot(n, i) * dot(n, i));
+    if (k < 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    return sub(scale(eta, i), scale(eta * dot(n, i) + sqrtf(k), n));
+}
+__device__ __forceinline__ float rt_min(float a, float b) { return b < a ? b : a; }
+__device__ __forceinline__ float rt_max(float a, float b) { return b > a ? b : a; }
+__device__ __forceinline__ float dot4(float4 r, float x, float y, float z, float w) {
+    return r.x * x + r.y * y + r.z * z + r.w * w;
+}
+__device__ __forceinline__ uint32_t bits(float f) { return __float_as_uint(f); }
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+template <int MATH> struct DevMath;
+template <> struct DevMath<MATH_PORTABLE> {
+    __device__ static float pow(float a, float b) { return pm_powf(a, b); }
+    __device__ static float acos(float a) { return pm_acosf(a); }
+    __device__ static float atan2(float a, float b) { return pm_atan2f(a, b); }
+    __device__ static void sincos(float a, float* s, float* c) { pm_sincosf(a, s, c); }
+};
+template <> struct DevMath<MATH_DEVICE> {
+    __device__ static float pow(float a, float b) { return powf(a, b); }
+    __device__ static float acos(float a) { return acosf(a); }
+    __device__ static float atan2(float a, float b) { return atan2f(a, b); }
+    __device__ static void sincos(float a, float* s, float* c) { sincosf(a, s, c); }
+};
+
+// ---- RNG (random.hip.h:14-30, 47-63, 83-95) -------------------------------
+struct Rng {
+    uint32_t state;
+    __device__ __forceinline__ uint32_t next() {
+        uint32_t old_state = state + 747796405u + 2891336453u;
+        uint32_t word = ((old_state >> ((old_state >> 28) + 4)) ^ old_state) * 277803737u;
+        state = (word >> 22) ^ word;
+        return state;
+    }
+    __device__ __forceinline__ float f() { return __uint2float_rn(next()) * (1.0f / 4294967296.0f); }
+    template <int MATH> __device__ __forceinline__ f3 in_unit_sphere() {
+        float r = DevMath<MATH>::pow(f(), 0.33333f);
+        float theta = 3.14159265358979f * f();
+        float phi = 2.0f * 3.14159265358979f * f();
+        float st, ct, sp, cp;
+        DevMath<MATH>::sincos(theta, &st, &ct);
+        DevMath<MATH>::sincos(phi, &sp, &cp);
+        return mk(r * st * cp, r * st * sp, r * ct);
+    }
+    template <int MATH> __device__ __forceinline__ f3 in_unit_disk() {
+        float r = sqrtf(f());
+        float alpha = 2.0f * 3.14159265358979f * f();
+        float sa, ca;
+        DevMath<MATH>::sincos(alpha, &sa, &ca);
+        return mk(r * ca, r * sa, 0.0f);
+    }
+};
+
+// ---- traversal (bvh.hip.h:43-143, 145-276) ------------------------------------
+__device__ __forceinline__ f3 safe_invdir(f3 d) {
+    const float eps = 1e-5f;
+    float x = fabsf(d.x) > eps ? d.x : (d.x < 0.0f ? -eps : eps);
+    float y = fabsf(d.y) > eps ? d.y : (d.y < 0.0f ? -eps : eps);
+    float z = fabsf(d.z) > eps ? d.z : (d.z < 0.0f ? -eps : eps);
+    return mk(1.0f / x, 1.0f / y, 1.0f / z);
+}
+
+__device__ __forceinline__ bool aabb_hit(float4 mn, float4 mx, f3 inv, f3 oxinv, float t_min, float t_max) {
+    float fx = mx.x * inv.x + oxinv.x, fy = mx.y * inv.y + oxinv.y, fz = mx.z * inv.z + oxinv.z;
+    float nx = mn.x * inv.x + oxinv.x, ny = mn.y * inv.y + oxinv.y, nz = mn.z * inv.z + oxinv.z;
+    float max_t = fminf(rt_min(rt_min(rt_max(fx, nx), rt_max(fy, ny)), rt_max(fz, nz)), t_max);
+    float min_t = fmaxf(rt_max(rt_max(rt_min(fx, nx), rt_min(fy, ny)), rt_min(fz, nz)), t_min);
+    return min_t <= max_t;
+}
+
+struct HitRec {
+    float t;
+    uint32_t material;
+    uint32_t type;   // ORN_NODE_SPHERE / ORN_NODE_MESH
+    uint32_t inv;    // inverse transform index
+    uint32_t tri;    // 3 * triangle id
+    float u, v;
+};
+
+struct VisitCount {
+    uint32_t visits, internal, sphere, mesh, tri;
+};
+
+// Closest hit of one ray; returns whether anything was hit.  `err` gets
+// ERR_* bits when the ray is abandoned (the result is then a miss).
+template <bool COUNT>
+__device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, float t_min,
+                                          HitRec* out, VisitCount* vc, uint32_t* err) {
+    float t_max = (float)3.40282e+38;
+    uint32_t stack[kStackSize];
+    int sp = 0;
+    uint32_t node = sc.tlas_len - 1;
+    bool in_blas = false;
+    int blas_sp = 0;
+    f3 o = ro, d = rd;
+    f3 inv = safe_invdir(d);
+    f3 oxinv = mul(neg(o), inv);
+    const f3 winv = inv, woxinv = oxinv;
+    uint32_t material = 0, inv_id = 0;
+    bool any = false;
+    uint32_t visits = 0;
+    for (;;) {
+        if (++visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; return false; }
+        const float4* np = sc.nodes + 4 * (size_t)node;
+        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
+        uint32_t type = bits(c.w);
+        bool have_next = false;
+        uint32_t next = 0;
+        if (type == ORN_NODE_INTERNAL) {
+            if (COUNT) vc->internal++;
+            bool hl = aabb_hit(a, b, inv, oxinv, t_min, t_max);
+            bool hr = aabb_hit(c, e, inv, oxinv, t_min, t_max);
+            if (hr) {
+                next = bits(b.w);
+                have_next = true;
+                if (hl) {
+                    if (sp >= kStackSize) { *err |= ERR_STACK; return false; }
+                    stack[sp++] = bits(a.w);
+                }
+            } else if (hl) {
+                next = bits(a.w);
+                have_next = true;
+            }
+        } else if (type == ORN_NODE_TRIANGLE) {
+            if (COUNT) vc->tri++;
+            // Möller–Trumbore exactly as bvh.hip.h:72-117 (e1, e2 precomputed)
+            f3 v1 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
+            f3 s1 = cross(d, e2);
+            float det = dot(s1, e1);
+            float invd = 1.0f / det;
+            f3 dd = sub(o, v1);
+            float u = dot(dd, s1) * invd;
+            if (!(u < 0.0f || u > 1.0f)) {
+                f3 s2 = cross(dd, e1);
+                float v = dot(d, s2) * invd;
+                if (!(v < 0.0f || u + v > 1.0f)) {
+                    float t = dot(e2, s2) * invd;
+                    if (!(t < t_min || t > t_max) && t < t_max) {
+                        any = true;
+                        t_max = t;
+                        out->t = t;
+                        out->material = material;
+                        out->type = ORN_NODE_MESH;
+                        out->inv = inv_id;
+                        out->tri = bits(a.w) * 3u;
+                        out->u = u;
+                        out->v = v;
+                    }
+                }
+            }
+        } else if (type == ORN_NODE_SPHERE || type == ORN_NODE_MESH) {
+            // inverse rows 0..2: a, b, (c.xyz, e.x)
+            float4 r2 = make_float4(c.x, c.y, c.z, e.x);
+            f3 to = mk(dot4(a, o.x, o.y, o.z, 1.0f), dot4(b, o.x, o.y, o.z, 1.0f),
+                       dot4(r2, o.x, o.y, o.z, 1.0f));
+            f3 td = mk(dot4(a, d.x, d.y, d.z, 0.0f), dot4(b, d.x, d.y, d.z, 0.0f),
+                       dot4(r2, d.x, d.y, d.z, 0.0f));
+            uint32_t mat = bits(e.y);
+            uint32_t inv_index = bits(e.z) * 2u;
+            if (type == ORN_NODE_SPHERE) {
+                if (COUNT) vc->sphere++;
+                // sphere_hit, unit sphere at the origin
+                float aa = td.x * td.x + td.y * td.y + td.z * td.z;
+                float half_b = dot(to, td);
+                float cc = (to.x * to.x + to.y * to.y + to.z * to.z) - 1.0f * 1.0f;
+                float disc = half_b * half_b - aa * cc;
+                float t = t_max;
+                if (!(disc < 0.0f)) {
+                    float sq = sqrtf(disc);
+                    t = (-half_b - sq) / aa;
+                    if (t < t_min || t_max < t) {
+                        t = (-half_b + sq) / aa;
+                        if (t < t_min || t_max < t) t = t_max;
+                    }
+                }
+                if (t < t_max) {
+                    any = true;
+                    t_max = t;
+                    out->t = t;
+                    out->material = mat;
+                    out->type = ORN_NODE_SPHERE;
+                    out->inv = inv_index;
+                }
+            } else {
+                if (COUNT) vc->mesh++;
+                in_blas = true;
+                blas_sp = sp;
+                inv_id = inv_index;
+                material = mat;
+                o = to;
+                d = td;
+                inv = safe_invdir(d);
+                oxinv = mul(neg(o), inv);
+                next = bits(e.w);
+                have_next = true;
+            }
+        }
+        if (!have_next) {
+            if (in_blas && sp == blas_sp) {
+                in_blas = false;
+                o = ro;
+                d = rd;
+                inv = winv;
+                oxinv = woxinv;
+            }
+            if (sp == 0) break;
+            next = stack[--sp];
+        }
+        node = next;
+    }
+    if (COUNT) vc->visits += visits;
+    return any;
+}
+
+// ---- texture fetch (material.hip.h:30-33) ---------------------------------------
+__device__ __forceinline__ int tex_index(float c, uint32_t n, bool clamp_mode) {
+    if (!(c == c)) c = 0.0f;
+    float x = clamp_mode ? floorf(c * (float)n) : floorf((c - floorf(c)) * (float)n);
+    if (x > (float)(n - 1)) x = (float)(n - 1);
+    if (x < 0.0f) x = 0.0f;
+    return (int)x;
+}
+
+__device__ __forceinline__ float half_bits_to_float(uint32_t h) {
+    return __half2float(__ushort_as_half((unsigned short)h));
+}
+
+__device__ __forceinline__ f3 tex_sample(const TexDesc& t, float u, float v, bool clamp_mode) {
+    int x = tex_index(u, t.width, clamp_mode), y = tex_index(v, t.height, clamp_mode);
+    const unsigned char* row = t.data + (size_t)y * t.pitch;
+    if (t.format == ORN_TEXEL_RGBA8) {
+        uint32_t p = __ldg((const unsigned int*)(row + (size_t)x * 4));
+        return mk((float)(p & 0xffu) / 255.0f, (float)((p >> 8) & 0xffu) / 255.0f,
+                  (float)((p >> 16) & 0xffu) / 255.0f);
+    }
+    uint2 p = __ldg((const uint2*)(row + (size_t)x * 8));
+    return mk(half_bits_to_float(p.x & 0xffffu), half_bits_to_float(p.x >> 16),
+              half_bits_to_float(p.y & 0xffffu));
+}
+
+struct SampleCount {
+    uint32_t rays, sphere_hits, mesh_hits, textured;
+};
+
+// ---- one sample (pathtracer.hip.cpp:72-146) -----------------------------------------
+template <int SEM, int MATH, bool COUNT>
+__device__ __forceinline__ f3 trace_sample(const SceneDev& sc, const orn_constant_params& cp,
+                                           uint32_t px, uint32_t py, Rng& rng, VisitCount* vc,
+                                           SampleCount* scn, uint32_t* err) {
+    typedef DevMath<MATH> M;
+    float u = ((float)px + rng.f()) / (float)(cp.width - 1);
+    float v = ((float)py + rng.f()) / (float)(cp.height - 1);
+    const orn_camera& cam = cp.camera;
+    f3 disk = rng.in_unit_disk<MATH>();
+    f3 rdv = scale(cam.lens_radius, disk);
+    f3 cu = mk(cam.u[0], cam.u[1], cam.u[2]), cv = mk(cam.v[0], cam.v[1], cam.v[2]);
+    f3 origin = mk(cam.origin[0], cam.origin[1], cam.origin[2]);
+    f3 offset = add(scale(rdv.x, cu), scale(rdv.y, cv));
+    f3 llc = mk(cam.lower_left_corner[0], cam.lower_left_corner[1], cam.lower_left_corner[2]);
+    f3 hor = mk(cam.horizontal[0], cam.horizontal[1], cam.horizontal[2]);
+    f3 ver = mk(cam.vertical[0], cam.vertical[1], cam.vertical[2]);
+    f3 ro = add(origin, offset);
+    f3 rd = sub(sub(add(add(llc, scale(u, hor)), scale(v, ver)), origin), offset);
+    f3 color = mk(1.0f, 1.0f, 1.0f);
+    for (uint32_t i = 0; i < cp.depth; ++i) {
+        HitRec h;
+        h.tri = 0;
+        h.u = 0.0f;
+        h.v = 0.0f;
+        if (COUNT) scn->rays++;
+        if (!trace_ray<COUNT>(sc, ro, rd, cp.ray_cast_epsilon, &h, vc, err)) {
+            if (*err) return mk(0.0f, 0.0f, 0.0f);
+            f3 ud = normalize(rd);
+            float tt = 0.5f * (ud.y + 1.0f);
+            f3 sky = add(scale(1.0f - tt, mk(1.0f, 1.0f, 1.0f)), scale(tt, mk(0.5f, 0.7f, 1.0f)));
+            color = mul(color, sky);
+            break;
+        }
+        uint32_t transform_id = h.inv + 1u;
+        f3 hp = add(ro, scale(h.t, rd));
+        f3 normal;
+        bool front;
+        float hu, hv;
+        if (h.type == ORN_NODE_SPHERE) {
+            if (COUNT) scn->sphere_hits++;
+            const float4* m = sc.xforms + 4 * (size_t)transform_id;
+            f3 center = mk(dot4(ldg4(m), 0.0f, 0.0f, 0.0f, 1.0f), dot4(ldg4(m + 1), 0.0f, 0.0f, 0.0f, 1.0f),
+                           dot4(ldg4(m + 2), 0.0f, 0.0f, 0.0f, 1.0f));
+            f3 on = normalize(sub(hp, center));
+            float theta = M::acos(-on.y);
+            float phi = M::atan2(-on.z, on.x) + 3.14159265358979f;
+            hu = phi / (2.0f * 3.14159265358979f);
+            hv = theta / 3.14159265358979f;
+            if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
+            else { normal = on; front = true; }
+        } else {
+            if (COUNT) scn->mesh_hits++;
+            float4 n0 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri));
+            float4 n1 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri + 1));
+            float4 n2 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri + 2));
+            float2 t0 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri));
+            float2 t1 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri + 1));
+            float2 t2 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri + 2));
+            float w = 1.0f - h.u - h.v;
+            float nx = w * n0.x + h.u * n1.x + h.v * n2.x;
+            float ny = w * n0.y + h.u * n1.y + h.v * n2.y;
+            float nz = w * n0.z + h.u * n1.z + h.v * n2.z;
+            hu = w * t0.x + h.u * t1.x + h.v * t2.x;
+            hv = w * t0.y + h.u * t1.y + h.v * t2.y;
+            const float4* m = sc.xforms + 4 * (size_t)h.inv;
+            float4 m0 = ldg4(m), m1 = ldg4(m + 1), m2 = ldg4(m + 2), m3 = ldg4(m + 3);
+            f3 tn = mk(m0.x * nx + m1.x * ny + m2.x * nz + m3.x * 0.0f,
+                       m0.y * nx + m1.y * ny + m2.y * nz + m3.y * 0.0f,
+                       m0.z * nx + m1.z * ny + m2.z * nz + m3.z * 0.0f);
+            f3 on = normalize(tn);
+            if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
+            else { normal = on; front = true; }
+        }
+        float4 ma = ldg4(sc.materials + 2 * (size_t)h.material);
+        float4 mb = ldg4(sc.materials + 2 * (size_t)h.material + 1);
+        uint32_t mtype = bits(mb.z);
+        uint32_t tex_id = bits(ma.w);
+        bool use_tex = SEM == SEM_WGSL ? (tex_id < cp.textures_count && tex_id < sc.textures_len)
+                                       : tex_id < sc.textures_len;
+        if (mtype == ORN_LAMBERTIAN) {
+            f3 dir = add(normal, normalize(rng.in_unit_sphere<MATH>()));
+            if (fabsf(dir.x) < 1e-8f && fabsf(dir.y) < 1e-8f && fabsf(dir.z) < 1e-8f) dir = normal;
+            f3 att = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
+            if (COUNT && use_tex) scn->textured++;
+            ro = hp;
+            rd = dir;
+            color = mul(color, att);
+        } else if (mtype == ORN_METAL) {
+            f3 dir = add(reflect(normalize(rd), normal), scale(mb.x, rng.in_unit_sphere<MATH>()));
+            f3 att = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
+            if (COUNT && use_tex) scn->textured++;
+            if (SEM == SEM_WGSL && !(dot(dir, normal) > 0.0f)) {
+                color = mul(color, mk(0.0f, 0.0f, 0.0f));
+                break;
+            }
+            ro = hp;
+            rd = dir;
+            color = mul(color, att);
+        } else if (mtype == ORN_DIELECTRIC) {
+            float ior = mb.y;
+            float ratio = front ? 1.0f / ior : ior;
+            f3 ud = normalize(rd);
+            float cos_t = fminf(dot(neg(ud), normal), 1.0f);
+            float sin_t = sqrtf(1.0f - cos_t * cos_t);
+            bool refl = ratio * sin_t > 1.0f;
+            if (!refl) {
+                float r0 = (1.0f - ratio) / (1.0f + ratio);
+                r0 = r0 * r0;
+                float p = r0 + (1.0f - r0) * M::pow(1.0f - cos_t, 5.0f);
+                refl = p > rng.f();
+            }
+            f3 dir = refl ? reflect(ud, normal) : refract(ud, normal, ratio);
+            ro = hp;
+            rd = dir;
+            color = mul(color, mk(1.0f, 1.0f, 1.0f));
+        } else {
+            f3 em = mk(0.0f, 0.0f, 0.0f);
+            if (mtype == ORN_DIFFUSE_LIGHT) {
+                em = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
+                if (COUNT && use_tex) scn->textured++;
+            }
+            color = mul(color, em);
+            break;
+        }
+    }
+    return color;
+}
+
+// post_processing (pathtracer.hip.cpp:58-70; pathtracer.wgsl:81-93)
+template <int SEM, int MATH>
+__device__ __forceinline__ float4 post_process(float4 acc, float ci, float inv_gamma) {
+    float q[4] = {acc.x / ci, acc.y / ci, acc.z / ci, acc.w / ci};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        q[k] = SEM == SEM_WGSL ? fminf(fmaxf(q[k], 0.0f), 1.0f) : fmaxf(fminf(q[k], 1.0f), 0.0f);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[k] = DevMath<MATH>::pow(q[k], inv_gamma);
+    return make_float4(q[0], q[1], q[2], q[3]);
+}
+
+}  // namespace orn

@@ -1,0 +1,45 @@
+// pt_scene.h — device-resident scene description shared by the host C ABI
+// and the kernels.
+//
+// Node layout in HBM (one array, TLAS nodes [0, tlas_len), BLAS nodes
+// after them with every BLAS id offset by tlas_len), four float4 per node:
+//   internal  a=(left.min, left id)  b=(left.max, right id)
+//             c=(right.min, type=0)  e=(right.max, 0)
+//   triangle  a=(v0, triangle id)    b=(v1-v0, 0)  c=(v2-v0, type=3)  e=0
+//   sphere    a,b=inverse rows 0,1   c=(inverse row 2 xyz, type=1)
+//             e=(inverse row 2 w, material, transform id, 0)
+//   mesh      as sphere with type=2 and e.w = BLAS root id
+// (BvhNode, src/gpu_structs.zig:22-31, carries the same information; the
+// leaf's own AABB, unused by traversal, is replaced by the transform rows.)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace orn {
+
+enum { SEM_HIP = 0, SEM_WGSL = 1 };          // enum orn_semantics
+enum { MATH_PORTABLE = 0, MATH_DEVICE = 1 };  // transcendental implementation
+// Error bits written to the context's device error word.
+enum { ERR_STACK = 1u, ERR_VISITS = 2u };
+
+struct TexDesc {
+    const unsigned char* data;
+    uint32_t width, height, pitch, format;
+};
+
+struct SceneDev {
+    const float4* nodes;        // 4 float4 per node, TLAS then BLAS
+    uint32_t tlas_len;
+    uint32_t node_count;
+    const float4* xforms;       // 4 float4 per matrix, blob transforms as given
+    const float4* normals;
+    const uint32_t* normal_indices;
+    const float2* uvs;
+    const uint32_t* uv_indices;
+    const float4* materials;    // 2 float4 per material
+    const TexDesc* textures;
+    uint32_t textures_len;
+};
+
+}  // namespace orn
