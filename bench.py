@@ -201,6 +201,21 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def reduce_max(values, dist, device="cpu"):
+    """Max over ranks of each timing (the slowest rank bounds the job)."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_throughput(world, samples_per_step, steps, total_ms):
+    """Whole-job Msamples/s: every rank renders its own replica of the frame."""
+    return world * samples_per_step * steps / (total_ms / 1e3) / 1e6
+
+
 def run_ours(args):
     import torch
     from zig_ornament_gb300 import _lib, ornament
@@ -280,12 +295,9 @@ def run_ours(args):
     samples_step = n_px * args.spp
     total_ms = float(sum(step_ms))
     total_e2e = float(sum(e2e_ms))
-    if dist:
-        t = torch.tensor([total_ms, total_e2e], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, total_e2e = float(t[0]), float(t[1])
-    value = world * samples_step * args.steps / (total_ms / 1e3) / 1e6
-    e2e_value = world * samples_step * args.steps / (total_e2e / 1e3) / 1e6
+    total_ms, total_e2e = reduce_max([total_ms, total_e2e], dist, device=f"cuda:{local}")
+    value = job_throughput(world, samples_step, args.steps, total_ms)
+    e2e_value = job_throughput(world, samples_step, args.steps, total_e2e)
     if rank != 0:
         if dist:
             dist.destroy_process_group()

@@ -20,13 +20,17 @@ def bits(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
+KERNELS = [_lib.KERNEL_MEGA, _lib.KERNEL_WAVEFRONT]
+KERNEL_IDS = ["mega", "wavefront"]
+
+
 def make_state(depth=8, gamma=1.0, flip=False, iterations=1, semantics=_lib.SEMANTICS_HIP, spp_per_launch=0,
-               eps=0.001):
+               eps=0.001, kernel=_lib.KERNEL_MEGA):
     s = _lib.State()
     s.depth, s.flip_y = depth, 1 if flip else 0
     s.inverted_gamma = float(np.float32(1.0) / np.float32(gamma))
     s.iterations, s.ray_cast_epsilon = iterations, eps
-    s.semantics, s.kernel, s.spp_per_launch = semantics, _lib.KERNEL_MEGA, spp_per_launch
+    s.semantics, s.kernel, s.spp_per_launch = semantics, kernel, spp_per_launch
     return s
 
 
@@ -56,7 +60,8 @@ def _flip_rows(fb, flip):
     return fb.reshape(H, -1, 4)[::-1].reshape(-1, 4) if flip else fb
 
 
-def test_render_matches_reference_pmath(golden, golden_camera, golden_renderer):
+@pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)
+def test_render_matches_reference_pmath(golden, golden_camera, golden_renderer, kernel):
     """PathTracer.render semantics end to end: the fused single pass, a
     multi-pass render, a continued (progressive) render, flip_y + gamma."""
     r = golden_renderer
@@ -64,7 +69,7 @@ def test_render_matches_reference_pmath(golden, golden_camera, golden_renderer):
     states = {}
     for name, spp, ci, depth, gamma, flip, base in _golden_cases(golden):
         r.set_resolution(W, H)          # fresh target: RNG reseeded with the pixel index
-        r.set_state(make_state(depth=depth, gamma=gamma, flip=flip, iterations=spp))
+        r.set_state(make_state(depth=depth, gamma=gamma, flip=flip, iterations=spp, kernel=kernel))
         r.set_camera(golden_camera)
         if base:
             acc0, rng0 = states[base]
@@ -80,11 +85,12 @@ def test_render_matches_reference_pmath(golden, golden_camera, golden_renderer):
         assert np.array_equal(bits(fb), bits(_flip_rows(golden[key + "_fb"], flip))), name
 
 
+@pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)
 @pytest.mark.parametrize("spp_per_launch", [1, 2, 7])
-def test_launch_chunking_does_not_change_results(golden_camera, golden_renderer, golden, spp_per_launch):
+def test_launch_chunking_does_not_change_results(golden_camera, golden_renderer, golden, spp_per_launch, kernel):
     r = golden_renderer
     r.set_resolution(W, H)
-    r.set_state(make_state(gamma=2.2, iterations=5, spp_per_launch=spp_per_launch))
+    r.set_state(make_state(gamma=2.2, iterations=5, spp_per_launch=spp_per_launch, kernel=kernel))
     r.set_camera(golden_camera)
     r.render()
     acc, rng, _ = r.progress()
@@ -92,11 +98,12 @@ def test_launch_chunking_does_not_change_results(golden_camera, golden_renderer,
     assert np.array_equal(rng, golden["render_pmath_pass5_rng"])
 
 
+@pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)
 @pytest.mark.parametrize("semantics", [_lib.SEMANTICS_HIP, _lib.SEMANTICS_WGSL])
-def test_semantics_vs_oracle(golden_bvh, golden_camera, golden_renderer, oracle, semantics):
+def test_semantics_vs_oracle(golden_bvh, golden_camera, golden_renderer, oracle, semantics, kernel):
     r = golden_renderer
     r.set_resolution(W, H)
-    r.set_state(make_state(depth=10, gamma=2.2, iterations=4, semantics=semantics))
+    r.set_state(make_state(depth=10, gamma=2.2, iterations=4, semantics=semantics, kernel=kernel))
     r.set_camera(golden_camera)
     r.render()
     acc, rng, _ = r.progress()
@@ -185,14 +192,15 @@ def test_pathtracer_surface_end_to_end(oracle):
     pt.deinit()
 
 
-def test_sphere_field_and_instanced_vs_oracle(oracle):
+@pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)
+def test_sphere_field_and_instanced_vs_oracle(oracle, kernel):
     for scene, w, h, depth in ((scenes.spheres_scene(80, 45, seed=0), 80, 45, 10),
                                (scenes.instanced_meshes_scene(96, 54, seed=1, n_blas=4, n_instances=40,
                                                               tri_range=(2000, 8000), texture_size=128), 96, 54, 8)):
         bvh = ornament.Bvh(scene)
         r = ornament.Renderer(bvh, device=0)
         r.set_resolution(w, h)
-        r.set_state(make_state(depth=depth, gamma=2.2, iterations=2))
+        r.set_state(make_state(depth=depth, gamma=2.2, iterations=2, kernel=kernel))
         r.set_camera(scene.camera.to_struct())
         r.render()
         acc, rng, _ = r.progress()
@@ -231,8 +239,42 @@ def test_primary_hits_instanced_1080p_scene(oracle):
     r.close()
 
 
+@pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)
+def test_depth_zero_and_one(golden_bvh, golden_camera, golden_renderer, oracle, kernel):
+    """Edge cases of the bounce loop: depth 0 (no ray at all: every sample is
+    white) and depth 1 (camera rays only)."""
+    r = golden_renderer
+    for depth in (0, 1):
+        r.set_resolution(W, H)
+        r.set_state(make_state(depth=depth, iterations=3, kernel=kernel))
+        r.set_camera(golden_camera)
+        r.render()
+        acc, rng, _ = r.progress()
+        cp = ol.make_params(golden_camera, W, H, depth=depth, textures_count=golden_bvh.scene_textures_count)
+        oacc, orng, _, _ = oracle.render(golden_bvh, cp, 3)
+        assert np.array_equal(rng, orng) and np.array_equal(bits(acc), bits(oacc)), depth
+    assert (oacc[:, :3] <= 3.0).all()
+
+
+def test_kernels_agree_at_1080p():
+    """Megakernel and wavefront give the same bits on the benchmark scene."""
+    scene = scenes.instanced_meshes_scene()
+    bvh = ornament.Bvh(scene)
+    out = []
+    for kernel in KERNELS:
+        r = ornament.Renderer(bvh, device=0)
+        r.set_resolution(1920, 1080)
+        r.set_state(make_state(iterations=2, kernel=kernel))
+        r.set_camera(scene.camera.to_struct())
+        r.render()
+        out.append(r.progress())
+        r.close()
+    assert np.array_equal(bits(out[0][0]), bits(out[1][0])) and np.array_equal(out[0][1], out[1][1])
+
+
 @pytest.mark.slow
-def test_full_size_properties_1080p():
+@pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)
+def test_full_size_properties_1080p(kernel):
     """Full-size (1920x1080) properties: deterministic, progressive renders
     equal one-shot renders, alpha counts the samples, values finite, work
     counters consistent."""
@@ -243,10 +285,10 @@ def test_full_size_properties_1080p():
     for r in (a, b):
         r.set_resolution(1920, 1080)
         r.set_camera(scene.camera.to_struct())
-    a.set_state(make_state(iterations=4))
+    a.set_state(make_state(iterations=4, kernel=kernel))
     a.enable_counters(True)
     a.render()
-    b.set_state(make_state(iterations=2))
+    b.set_state(make_state(iterations=2, kernel=kernel))
     b.render()
     b.render()
     acc_a, rng_a, ci_a = a.progress()

@@ -48,6 +48,13 @@ struct orn_context {
     uint32_t* rng = nullptr;
 
     uint32_t* d_error = nullptr;
+    uint32_t* d_work = nullptr;
+    // wavefront path pool (allocated on first use)
+    uint32_t wf_slots = 0;
+    std::vector<void*> wf_allocs;
+    orn::WaveLaunch wf{};
+    uint32_t* wf_host_stat = nullptr;     // pinned ring of [count, pending] pairs
+    cudaEvent_t wf_events[16] = {};
     unsigned long long* d_counters = nullptr;
     bool counters_enabled = false;
     bool rendered = false;
@@ -259,6 +266,92 @@ orn_constant_params make_params(const orn_context* ctx, float current_iteration)
     return cp;
 }
 
+constexpr int kWfRing = 16;
+constexpr int kWfLag = 6;
+
+// Allocates the wavefront path pool: min(pixels, 2^20) slots of structure-of-
+// arrays path state (about 120 bytes each) plus the ray queue.
+int ensure_wavefront(orn_context* ctx) {
+    const uint32_t pixels = ctx->width * ctx->height;
+    uint32_t want = std::min<uint32_t>(pixels, 1u << 20);
+    want = (want + 255) / 256 * 256;
+    if (ctx->wf_slots >= want) return ORN_OK;
+    for (void* p : ctx->wf_allocs) cudaFree(p);
+    ctx->wf_allocs.clear();
+    ctx->wf_slots = 0;
+    auto alloc = [&](size_t bytes, void** out) -> int {
+        ORN_CUDA(ctx, cudaMalloc(out, bytes));
+        ctx->wf_allocs.push_back(*out);
+        return ORN_OK;
+    };
+    orn::WaveLaunch& w = ctx->wf;
+    int st;
+    if ((st = alloc(4 * sizeof(uint32_t), (void**)&w.pixel_counter))) return st;
+    if ((st = alloc(16 * sizeof(uint32_t), (void**)&w.qstat))) return st;
+    if ((st = alloc((size_t)want * 4, (void**)&w.queue))) return st;
+    if ((st = alloc((size_t)want * 4, (void**)&w.mode))) return st;
+    if ((st = alloc((size_t)want * 4, (void**)&w.pixel))) return st;
+    if ((st = alloc((size_t)want * 8, (void**)&w.kb))) return st;
+    if ((st = alloc((size_t)want * 4, (void**)&w.rng_state))) return st;
+    if ((st = alloc((size_t)want * 16, (void**)&w.accum))) return st;
+    if ((st = alloc((size_t)want * 16, (void**)&w.color))) return st;
+    if ((st = alloc((size_t)want * 16, (void**)&w.ro))) return st;
+    if ((st = alloc((size_t)want * 16, (void**)&w.rd))) return st;
+    if ((st = alloc((size_t)want * 32, (void**)&w.hit))) return st;
+    if (!ctx->wf_host_stat) {
+        ORN_CUDA(ctx, cudaMallocHost(&ctx->wf_host_stat, kWfRing * 2 * sizeof(uint32_t)));
+        for (int i = 0; i < kWfRing; ++i)
+            ORN_CUDA(ctx, cudaEventCreateWithFlags(&ctx->wf_events[i], cudaEventDisableTiming));
+    }
+    ctx->wf_slots = want;
+    return ORN_OK;
+}
+
+// One sweep of the wavefront over every pixel: `spp` passes starting at
+// current_iteration = cp.current_iteration.  Iterations (logic, readback of
+// the queue length, extend) are issued ahead of the GPU; the loop stops once
+// an iteration kWfLag back produced no ray and left no slot waiting.
+int render_wavefront_sweep(orn_context* ctx, const orn_constant_params& cp, uint32_t spp, bool do_post) {
+    orn::WaveLaunch& w = ctx->wf;
+    w.scene = ctx->scene;
+    w.cp = cp;
+    w.spp = spp;
+    w.do_post = do_post ? 1u : 0u;
+    w.pixel_count = ctx->width * ctx->height;
+    w.slots = ctx->wf_slots;
+    w.acc = ctx->acc;
+    w.fb = ctx->fb;
+    w.rng = ctx->rng;
+    w.error = ctx->d_error;
+    w.counters = ctx->d_counters;
+    w.fetch_threshold = orn::kFetchThreshold;
+    ORN_CUDA(ctx, cudaMemsetAsync(w.mode, 0, (size_t)w.slots * 4, ctx->stream));
+    ORN_CUDA(ctx, cudaMemsetAsync(w.pixel_counter, 0, 4 * sizeof(uint32_t), ctx->stream));
+    ORN_CUDA(ctx, cudaMemsetAsync(w.qstat, 0, 16 * sizeof(uint32_t), ctx->stream));
+    const int sem = (int)ctx->state.semantics;
+    // Upper bound on iterations: every ray of every sample of every pixel
+    // (protects against a logic error turning into an endless host loop).
+    const uint64_t max_iter = (uint64_t)spp * (ctx->state.depth + 1) *
+                                  ((w.pixel_count + w.slots - 1) / w.slots) + 64;
+    for (uint64_t it = 0;; ++it) {
+        if (it >= (uint64_t)kWfLag) {
+            const int r = (int)((it - kWfLag) % kWfRing);
+            ORN_CUDA(ctx, cudaEventSynchronize(ctx->wf_events[r]));
+            if (ctx->wf_host_stat[2 * r] == 0 && ctx->wf_host_stat[2 * r + 1] == 0) break;
+        }
+        if (it > max_iter) return fail(ctx, ORN_ERR_TIMEOUT, "wavefront did not drain");
+        const uint32_t iter = (uint32_t)it;
+        ORN_CUDA(ctx, orn::launch_wf_logic(w, iter, sem, orn::MATH_PORTABLE, ctx->counters_enabled, ctx->stream));
+        const int r = (int)(it % kWfRing);
+        ORN_CUDA(ctx, cudaMemcpyAsync(ctx->wf_host_stat + 2 * r, w.qstat + 4 * (iter & 3), 2 * sizeof(uint32_t),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+        ORN_CUDA(ctx, cudaEventRecord(ctx->wf_events[r], ctx->stream));
+        ORN_CUDA(ctx, orn::launch_wf_extend(w, iter, ctx->counters_enabled, ctx->stream));
+        ctx->launches += 2;
+    }
+    return ORN_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -306,6 +399,7 @@ int orn_create(const orn_scene_blob* blob, int device, orn_context** out) {
         ORN_CUDA(ctx, cudaEventCreate(&ctx->ev_stop));
         ORN_CUDA(ctx, cudaMalloc(&ctx->d_error, 4));
         ORN_CUDA(ctx, cudaMemset(ctx->d_error, 0, 4));
+        ORN_CUDA(ctx, cudaMalloc(&ctx->d_work, 4));
         ORN_CUDA(ctx, cudaMalloc(&ctx->d_counters, ORN_COUNTER_COUNT * sizeof(unsigned long long)));
         ORN_CUDA(ctx, cudaMemset(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long)));
         std::vector<float4> nodes;
@@ -381,7 +475,12 @@ int orn_destroy(orn_context* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_target(ctx);
     for (void* p : ctx->scene_allocs) cudaFree(p);
+    for (void* p : ctx->wf_allocs) cudaFree(p);
+    if (ctx->wf_host_stat) cudaFreeHost(ctx->wf_host_stat);
+    for (cudaEvent_t e : ctx->wf_events)
+        if (e) cudaEventDestroy(e);
     if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->d_work) cudaFree(ctx->d_work);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
@@ -465,17 +564,28 @@ int orn_render(orn_context* ctx) {
     p.rng = ctx->rng;
     p.error = ctx->d_error;
     p.counters = ctx->d_counters;
+    p.work_counter = ctx->d_work;
+    p.shade_threshold = orn::kShadeThreshold;
     if (ctx->counters_enabled)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long), ctx->stream));
+    if (ctx->state.kernel == ORN_KERNEL_WAVEFRONT) {
+        st = ensure_wavefront(ctx);
+        if (st) return st;
+    }
     ORN_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
     for (uint32_t done = 0; done < passes;) {
         uint32_t n = std::min(chunk, passes - done);
         p.cp = make_params(ctx, ci_start + (float)done);
         p.spp = n;
         p.do_post = (done + n == passes) ? 1u : 0u;
-        ORN_CUDA(ctx, orn::launch_mega(p, (int)ctx->state.semantics, orn::MATH_PORTABLE,
-                                       ctx->counters_enabled, ctx->stream));
-        ctx->launches++;
+        if (ctx->state.kernel == ORN_KERNEL_WAVEFRONT) {
+            st = render_wavefront_sweep(ctx, p.cp, n, p.do_post != 0);
+            if (st) return st;
+        } else {
+            ORN_CUDA(ctx, orn::launch_mega(p, (int)ctx->state.semantics, orn::MATH_PORTABLE,
+                                           ctx->counters_enabled, ctx->stream));
+            ctx->launches++;
+        }
         done += n;
     }
     ORN_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));

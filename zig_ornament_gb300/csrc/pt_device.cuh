@@ -137,11 +137,33 @@ struct VisitCount {
 
 // Closest hit of one ray; returns whether anything was hit.  `err` gets
 // ERR_* bits when the ray is abandoned (the result is then a miss).
-template <bool COUNT>
+// Traversal stack: the first SS entries live in shared memory (entry i of
+// this thread at sstack[i * sstride], so a warp's accesses hit 32 distinct
+// banks), deeper entries spill to a per-thread local array; the total depth
+// is the reference's 64.
+template <int SS>
+struct TravStack {
+    uint32_t* sstack;
+    int sstride;
+    uint32_t lstack[kStackSize - SS > 0 ? kStackSize - SS : 1];
+    __device__ __forceinline__ void put(int i, uint32_t v) {
+        if (SS >= kStackSize || i < SS) sstack[i * sstride] = v;
+        else lstack[i - SS] = v;
+    }
+    __device__ __forceinline__ uint32_t get(int i) const {
+        if (SS >= kStackSize || i < SS) return sstack[i * sstride];
+        return lstack[i - SS];
+    }
+};
+
+template <bool COUNT, int SS>
 __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, float t_min,
-                                          HitRec* out, VisitCount* vc, uint32_t* err) {
+                                          HitRec* out, VisitCount* vc, uint32_t* err,
+                                          uint32_t* sstack, int sstride) {
     float t_max = (float)3.40282e+38;
-    uint32_t stack[kStackSize];
+    TravStack<SS> stack;
+    stack.sstack = sstack;
+    stack.sstride = sstride;
     int sp = 0;
     uint32_t node = sc.tlas_len - 1;
     bool in_blas = false;
@@ -169,7 +191,7 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
                 have_next = true;
                 if (hl) {
                     if (sp >= kStackSize) { *err |= ERR_STACK; return false; }
-                    stack[sp++] = bits(a.w);
+                    stack.put(sp++, bits(a.w));
                 }
             } else if (hl) {
                 next = bits(a.w);
@@ -258,7 +280,7 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
                 oxinv = woxinv;
             }
             if (sp == 0) break;
-            next = stack[--sp];
+            next = stack.get(--sp);
         }
         node = next;
     }
@@ -296,12 +318,12 @@ struct SampleCount {
     uint32_t rays, sphere_hits, mesh_hits, textured;
 };
 
-// ---- one sample (pathtracer.hip.cpp:72-146) -----------------------------------------
-template <int SEM, int MATH, bool COUNT>
-__device__ __forceinline__ f3 trace_sample(const SceneDev& sc, const orn_constant_params& cp,
-                                           uint32_t px, uint32_t py, Rng& rng, VisitCount* vc,
-                                           SampleCount* scn, uint32_t* err) {
-    typedef DevMath<MATH> M;
+// ---- one sample (pathtracer.hip.cpp:72-146), in pieces ----------------------
+// Camera ray for pixel (px, py): 2 jitter draws, then the lens-disk draws
+// (camera.hip.h:25-33), consumed even when the aperture is 0.
+template <int MATH>
+__device__ __forceinline__ void camera_ray(const orn_constant_params& cp, uint32_t px, uint32_t py, Rng& rng,
+                                           f3* ro, f3* rd) {
     float u = ((float)px + rng.f()) / (float)(cp.width - 1);
     float v = ((float)py + rng.f()) / (float)(cp.height - 1);
     const orn_camera& cam = cp.camera;
@@ -313,8 +335,134 @@ __device__ __forceinline__ f3 trace_sample(const SceneDev& sc, const orn_constan
     f3 llc = mk(cam.lower_left_corner[0], cam.lower_left_corner[1], cam.lower_left_corner[2]);
     f3 hor = mk(cam.horizontal[0], cam.horizontal[1], cam.horizontal[2]);
     f3 ver = mk(cam.vertical[0], cam.vertical[1], cam.vertical[2]);
-    f3 ro = add(origin, offset);
-    f3 rd = sub(sub(add(add(llc, scale(u, hor)), scale(v, ver)), origin), offset);
+    *ro = add(origin, offset);
+    *rd = sub(sub(add(add(llc, scale(u, hor)), scale(v, ver)), origin), offset);
+}
+
+// Miss: sky gradient (pathtracer.hip.cpp:87-93).
+__device__ __forceinline__ f3 sky_color(f3 color, f3 rd) {
+    f3 ud = normalize(rd);
+    float tt = 0.5f * (ud.y + 1.0f);
+    f3 sky = add(scale(1.0f - tt, mk(1.0f, 1.0f, 1.0f)), scale(tt, mk(0.5f, 0.7f, 1.0f)));
+    return mul(color, sky);
+}
+
+// Hit shading and material (pathtracer.hip.cpp:95-145, material.hip.h):
+// returns true when the path continues with the scattered ray in (ro, rd),
+// false when it ends (emission or absorption) with `color` final.
+template <int SEM, int MATH, bool COUNT>
+__device__ __forceinline__ bool shade_hit(const SceneDev& sc, const orn_constant_params& cp, Rng& rng,
+                                          const HitRec& h, f3* ro_io, f3* rd_io, f3* color_io,
+                                          SampleCount* scn) {
+    typedef DevMath<MATH> M;
+    const f3 ro = *ro_io, rd = *rd_io;
+    f3 color = *color_io;
+    uint32_t transform_id = h.inv + 1u;
+    f3 hp = add(ro, scale(h.t, rd));
+    f3 normal;
+    bool front;
+    float hu, hv;
+    if (h.type == ORN_NODE_SPHERE) {
+        if (COUNT) scn->sphere_hits++;
+        const float4* m = sc.xforms + 4 * (size_t)transform_id;
+        f3 center = mk(dot4(ldg4(m), 0.0f, 0.0f, 0.0f, 1.0f), dot4(ldg4(m + 1), 0.0f, 0.0f, 0.0f, 1.0f),
+                       dot4(ldg4(m + 2), 0.0f, 0.0f, 0.0f, 1.0f));
+        f3 on = normalize(sub(hp, center));
+        float theta = M::acos(-on.y);
+        float phi = M::atan2(-on.z, on.x) + 3.14159265358979f;
+        hu = phi / (2.0f * 3.14159265358979f);
+        hv = theta / 3.14159265358979f;
+        if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
+        else { normal = on; front = true; }
+    } else {
+        if (COUNT) scn->mesh_hits++;
+        float4 n0 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri));
+        float4 n1 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri + 1));
+        float4 n2 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri + 2));
+        float2 t0 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri));
+        float2 t1 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri + 1));
+        float2 t2 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri + 2));
+        float w = 1.0f - h.u - h.v;
+        float nx = w * n0.x + h.u * n1.x + h.v * n2.x;
+        float ny = w * n0.y + h.u * n1.y + h.v * n2.y;
+        float nz = w * n0.z + h.u * n1.z + h.v * n2.z;
+        hu = w * t0.x + h.u * t1.x + h.v * t2.x;
+        hv = w * t0.y + h.u * t1.y + h.v * t2.y;
+        const float4* m = sc.xforms + 4 * (size_t)h.inv;
+        float4 m0 = ldg4(m), m1 = ldg4(m + 1), m2 = ldg4(m + 2), m3 = ldg4(m + 3);
+        f3 tn = mk(m0.x * nx + m1.x * ny + m2.x * nz + m3.x * 0.0f,
+                   m0.y * nx + m1.y * ny + m2.y * nz + m3.y * 0.0f,
+                   m0.z * nx + m1.z * ny + m2.z * nz + m3.z * 0.0f);
+        f3 on = normalize(tn);
+        if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
+        else { normal = on; front = true; }
+    }
+    float4 ma = ldg4(sc.materials + 2 * (size_t)h.material);
+    float4 mb = ldg4(sc.materials + 2 * (size_t)h.material + 1);
+    uint32_t mtype = bits(mb.z);
+    uint32_t tex_id = bits(ma.w);
+    bool use_tex = SEM == SEM_WGSL ? (tex_id < cp.textures_count && tex_id < sc.textures_len)
+                                   : tex_id < sc.textures_len;
+    if (mtype == ORN_LAMBERTIAN) {
+        f3 dir = add(normal, normalize(rng.in_unit_sphere<MATH>()));
+        if (fabsf(dir.x) < 1e-8f && fabsf(dir.y) < 1e-8f && fabsf(dir.z) < 1e-8f) dir = normal;
+        f3 att = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
+        if (COUNT && use_tex) scn->textured++;
+        *ro_io = hp;
+        *rd_io = dir;
+        *color_io = mul(color, att);
+        return true;
+    }
+    if (mtype == ORN_METAL) {
+        f3 dir = add(reflect(normalize(rd), normal), scale(mb.x, rng.in_unit_sphere<MATH>()));
+        f3 att = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
+        if (COUNT && use_tex) scn->textured++;
+        if (SEM == SEM_WGSL && !(dot(dir, normal) > 0.0f)) {
+            *color_io = mul(color, mk(0.0f, 0.0f, 0.0f));
+            return false;
+        }
+        *ro_io = hp;
+        *rd_io = dir;
+        *color_io = mul(color, att);
+        return true;
+    }
+    if (mtype == ORN_DIELECTRIC) {
+        float ior = mb.y;
+        float ratio = front ? 1.0f / ior : ior;
+        f3 ud = normalize(rd);
+        float cos_t = fminf(dot(neg(ud), normal), 1.0f);
+        float sin_t = sqrtf(1.0f - cos_t * cos_t);
+        bool refl = ratio * sin_t > 1.0f;
+        if (!refl) {
+            float r0 = (1.0f - ratio) / (1.0f + ratio);
+            r0 = r0 * r0;
+            float pr = r0 + (1.0f - r0) * M::pow(1.0f - cos_t, 5.0f);
+            refl = pr > rng.f();
+        }
+        f3 dir = refl ? reflect(ud, normal) : refract(ud, normal, ratio);
+        *ro_io = hp;
+        *rd_io = dir;
+        *color_io = mul(color, mk(1.0f, 1.0f, 1.0f));
+        return true;
+    }
+    f3 em = mk(0.0f, 0.0f, 0.0f);
+    if (mtype == ORN_DIFFUSE_LIGHT) {
+        em = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
+        if (COUNT && use_tex) scn->textured++;
+    }
+    *color_io = mul(color, em);
+    return false;
+}
+
+// One whole sample with the straightforward loop structure (used by the
+// debug kernels; the render kernel runs the same pieces as a state machine).
+template <int SEM, int MATH, bool COUNT, int SS>
+__device__ __forceinline__ f3 trace_sample(const SceneDev& sc, const orn_constant_params& cp,
+                                           uint32_t px, uint32_t py, Rng& rng, VisitCount* vc,
+                                           SampleCount* scn, uint32_t* err, uint32_t* sstack,
+                                           int sstride) {
+    f3 ro, rd;
+    camera_ray<MATH>(cp, px, py, rng, &ro, &rd);
     f3 color = mk(1.0f, 1.0f, 1.0f);
     for (uint32_t i = 0; i < cp.depth; ++i) {
         HitRec h;
@@ -322,105 +470,12 @@ __device__ __forceinline__ f3 trace_sample(const SceneDev& sc, const orn_constan
         h.u = 0.0f;
         h.v = 0.0f;
         if (COUNT) scn->rays++;
-        if (!trace_ray<COUNT>(sc, ro, rd, cp.ray_cast_epsilon, &h, vc, err)) {
+        if (!trace_ray<COUNT, SS>(sc, ro, rd, cp.ray_cast_epsilon, &h, vc, err, sstack, sstride)) {
             if (*err) return mk(0.0f, 0.0f, 0.0f);
-            f3 ud = normalize(rd);
-            float tt = 0.5f * (ud.y + 1.0f);
-            f3 sky = add(scale(1.0f - tt, mk(1.0f, 1.0f, 1.0f)), scale(tt, mk(0.5f, 0.7f, 1.0f)));
-            color = mul(color, sky);
+            color = sky_color(color, rd);
             break;
         }
-        uint32_t transform_id = h.inv + 1u;
-        f3 hp = add(ro, scale(h.t, rd));
-        f3 normal;
-        bool front;
-        float hu, hv;
-        if (h.type == ORN_NODE_SPHERE) {
-            if (COUNT) scn->sphere_hits++;
-            const float4* m = sc.xforms + 4 * (size_t)transform_id;
-            f3 center = mk(dot4(ldg4(m), 0.0f, 0.0f, 0.0f, 1.0f), dot4(ldg4(m + 1), 0.0f, 0.0f, 0.0f, 1.0f),
-                           dot4(ldg4(m + 2), 0.0f, 0.0f, 0.0f, 1.0f));
-            f3 on = normalize(sub(hp, center));
-            float theta = M::acos(-on.y);
-            float phi = M::atan2(-on.z, on.x) + 3.14159265358979f;
-            hu = phi / (2.0f * 3.14159265358979f);
-            hv = theta / 3.14159265358979f;
-            if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
-            else { normal = on; front = true; }
-        } else {
-            if (COUNT) scn->mesh_hits++;
-            float4 n0 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri));
-            float4 n1 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri + 1));
-            float4 n2 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri + 2));
-            float2 t0 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri));
-            float2 t1 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri + 1));
-            float2 t2 = __ldg(sc.uvs + __ldg(sc.uv_indices + h.tri + 2));
-            float w = 1.0f - h.u - h.v;
-            float nx = w * n0.x + h.u * n1.x + h.v * n2.x;
-            float ny = w * n0.y + h.u * n1.y + h.v * n2.y;
-            float nz = w * n0.z + h.u * n1.z + h.v * n2.z;
-            hu = w * t0.x + h.u * t1.x + h.v * t2.x;
-            hv = w * t0.y + h.u * t1.y + h.v * t2.y;
-            const float4* m = sc.xforms + 4 * (size_t)h.inv;
-            float4 m0 = ldg4(m), m1 = ldg4(m + 1), m2 = ldg4(m + 2), m3 = ldg4(m + 3);
-            f3 tn = mk(m0.x * nx + m1.x * ny + m2.x * nz + m3.x * 0.0f,
-                       m0.y * nx + m1.y * ny + m2.y * nz + m3.y * 0.0f,
-                       m0.z * nx + m1.z * ny + m2.z * nz + m3.z * 0.0f);
-            f3 on = normalize(tn);
-            if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
-            else { normal = on; front = true; }
-        }
-        float4 ma = ldg4(sc.materials + 2 * (size_t)h.material);
-        float4 mb = ldg4(sc.materials + 2 * (size_t)h.material + 1);
-        uint32_t mtype = bits(mb.z);
-        uint32_t tex_id = bits(ma.w);
-        bool use_tex = SEM == SEM_WGSL ? (tex_id < cp.textures_count && tex_id < sc.textures_len)
-                                       : tex_id < sc.textures_len;
-        if (mtype == ORN_LAMBERTIAN) {
-            f3 dir = add(normal, normalize(rng.in_unit_sphere<MATH>()));
-            if (fabsf(dir.x) < 1e-8f && fabsf(dir.y) < 1e-8f && fabsf(dir.z) < 1e-8f) dir = normal;
-            f3 att = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
-            if (COUNT && use_tex) scn->textured++;
-            ro = hp;
-            rd = dir;
-            color = mul(color, att);
-        } else if (mtype == ORN_METAL) {
-            f3 dir = add(reflect(normalize(rd), normal), scale(mb.x, rng.in_unit_sphere<MATH>()));
-            f3 att = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
-            if (COUNT && use_tex) scn->textured++;
-            if (SEM == SEM_WGSL && !(dot(dir, normal) > 0.0f)) {
-                color = mul(color, mk(0.0f, 0.0f, 0.0f));
-                break;
-            }
-            ro = hp;
-            rd = dir;
-            color = mul(color, att);
-        } else if (mtype == ORN_DIELECTRIC) {
-            float ior = mb.y;
-            float ratio = front ? 1.0f / ior : ior;
-            f3 ud = normalize(rd);
-            float cos_t = fminf(dot(neg(ud), normal), 1.0f);
-            float sin_t = sqrtf(1.0f - cos_t * cos_t);
-            bool refl = ratio * sin_t > 1.0f;
-            if (!refl) {
-                float r0 = (1.0f - ratio) / (1.0f + ratio);
-                r0 = r0 * r0;
-                float p = r0 + (1.0f - r0) * M::pow(1.0f - cos_t, 5.0f);
-                refl = p > rng.f();
-            }
-            f3 dir = refl ? reflect(ud, normal) : refract(ud, normal, ratio);
-            ro = hp;
-            rd = dir;
-            color = mul(color, mk(1.0f, 1.0f, 1.0f));
-        } else {
-            f3 em = mk(0.0f, 0.0f, 0.0f);
-            if (mtype == ORN_DIFFUSE_LIGHT) {
-                em = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
-                if (COUNT && use_tex) scn->textured++;
-            }
-            color = mul(color, em);
-            break;
-        }
+        if (!shade_hit<SEM, MATH, COUNT>(sc, cp, rng, h, &ro, &rd, &color, scn)) break;
     }
     return color;
 }

@@ -12,6 +12,7 @@
 namespace orn {
 
 constexpr int kMegaBlock = 128;
+constexpr int kSmemStack = 32;   // traversal-stack entries per thread kept in shared memory
 
 // Arguments of one megakernel launch (passed by value).
 struct RenderLaunch {
@@ -25,9 +26,51 @@ struct RenderLaunch {
     uint32_t* rng;
     uint32_t* error;
     unsigned long long* counters;
+    uint32_t* work_counter;    // next pixel to hand out (zeroed before each launch)
+    int shade_threshold;       // ready lanes needed before a warp shades
 };
 
+#ifndef ORN_SHADE_THRESHOLD
+#define ORN_SHADE_THRESHOLD 8
+#endif
+constexpr int kShadeThreshold = ORN_SHADE_THRESHOLD;
+
+// Arguments of one wavefront iteration (wavefront.cu).  Path slots are
+// structure-of-arrays; qstat holds per-iteration [queue count, slots waiting
+// for a pixel, queue head, unused] for four iterations in rotation.
+struct WaveLaunch {
+    SceneDev scene;
+    orn_constant_params cp;
+    uint32_t spp;
+    uint32_t do_post;
+    uint32_t pixel_count;
+    uint32_t slots;
+    float4* acc;
+    float4* fb;
+    uint32_t* rng;
+    uint32_t* error;
+    unsigned long long* counters;
+    uint32_t* pixel_counter;
+    uint32_t* qstat;
+    uint32_t* queue;
+    uint32_t* mode;
+    uint32_t* pixel;
+    uint2* kb;
+    uint32_t* rng_state;
+    float4* accum;
+    float4* color;
+    float4* ro;
+    float4* rd;
+    float4* hit;
+    int fetch_threshold;
+};
+
+constexpr int kFetchThreshold = 16;
+
 cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, cudaStream_t s);
+cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, int math, bool count,
+                            cudaStream_t s);
+cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, cudaStream_t s);
 cudaError_t launch_trace_rays(const SceneDev& sc, float t_min, const float* rays, size_t count,
                               orn_hit* hits, uint32_t* visits, uint32_t* error, cudaStream_t s);
 cudaError_t launch_seed_rng(uint32_t* rng, uint32_t n, cudaStream_t s);

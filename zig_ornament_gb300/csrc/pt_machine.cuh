@@ -1,0 +1,173 @@
+// pt_machine.cuh — the megakernel as a warp-synchronous state machine.
+//
+// A path tracer's work per sample varies by two orders of magnitude (a sky
+// pixel costs ~20 node visits, a pixel on a glass object several hundred),
+// and the nested loops of the straightforward form (samples → bounces →
+// traversal) let the lanes of a warp drift apart: measured with ncu on
+// sm_103a, the nested-loop megakernel ran with 1.08 active threads per warp.
+//
+// Here every lane holds one path and the warp runs ONE loop whose condition
+// comes from warp ballots, so the lanes stay converged:
+//   * each iteration, every lane in the TRAVERSE state visits one BVH node;
+//   * lanes whose ray finished traversal wait in SHADE until enough of the
+//     warp is ready (or nobody is traversing), then all ready lanes shade
+//     together (material scatter, next bounce, next sample, pixel done);
+//   * lanes without a pixel take the next ones from a global counter, one
+//     atomic per warp (persistent threads, dynamic load balance).
+// Each pixel's own sequence of operations is unchanged — the same RNG draws,
+// the same float operations in the same order — so the result is
+// bit-identical to the reference's per-pass loop.
+#pragma once
+
+#include "pt_device.cuh"
+
+namespace orn {
+
+// Traversal state of one ray, advanced one node per step
+// (bvh.hip.h:145-276 visit order; see trace_ray).
+struct Walker {
+    uint32_t node;
+    int sp;
+    int blas_sp;
+    bool in_blas;
+    bool any;
+    f3 o, d, inv, oxinv;
+    float t_max;
+    uint32_t material, inv_id;
+    uint32_t visits;
+};
+
+__device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 ro, f3 rd) {
+    w.node = sc.tlas_len - 1;
+    w.sp = 0;
+    w.blas_sp = 0;
+    w.in_blas = false;
+    w.any = false;
+    w.o = ro;
+    w.d = rd;
+    w.inv = safe_invdir(rd);
+    w.oxinv = mul(neg(ro), w.inv);
+    w.t_max = (float)3.40282e+38;
+    w.material = 0;
+    w.inv_id = 0;
+    w.visits = 0;
+}
+
+// Visits the current node; returns false when the traversal has finished.
+// The world-space inverse direction is recomputed on BLAS exit (the same
+// operations give the same bits) instead of being kept in registers.
+template <bool COUNT, int SS>
+__device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro, f3 rd, float t_min,
+                                            HitRec* out, TravStack<SS>& stack, VisitCount* vc,
+                                            uint32_t* err) {
+    if (++w.visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; w.any = false; return false; }
+    const float4* np = sc.nodes + 4 * (size_t)w.node;
+    float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
+    uint32_t type = bits(c.w);
+    bool have_next = false;
+    uint32_t next = 0;
+    if (type == ORN_NODE_INTERNAL) {
+        if (COUNT) vc->internal++;
+        bool hl = aabb_hit(a, b, w.inv, w.oxinv, t_min, w.t_max);
+        bool hr = aabb_hit(c, e, w.inv, w.oxinv, t_min, w.t_max);
+        if (hr) {
+            next = bits(b.w);
+            have_next = true;
+            if (hl) {
+                if (w.sp >= kStackSize) { *err |= ERR_STACK; w.any = false; return false; }
+                stack.put(w.sp++, bits(a.w));
+            }
+        } else if (hl) {
+            next = bits(a.w);
+            have_next = true;
+        }
+    } else if (type == ORN_NODE_TRIANGLE) {
+        if (COUNT) vc->tri++;
+        f3 v1 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
+        f3 s1 = cross(w.d, e2);
+        float det = dot(s1, e1);
+        float invd = 1.0f / det;
+        f3 dd = sub(w.o, v1);
+        float u = dot(dd, s1) * invd;
+        if (!(u < 0.0f || u > 1.0f)) {
+            f3 s2 = cross(dd, e1);
+            float v = dot(w.d, s2) * invd;
+            if (!(v < 0.0f || u + v > 1.0f)) {
+                float t = dot(e2, s2) * invd;
+                if (!(t < t_min || t > w.t_max) && t < w.t_max) {
+                    w.any = true;
+                    w.t_max = t;
+                    out->t = t;
+                    out->material = w.material;
+                    out->type = ORN_NODE_MESH;
+                    out->inv = w.inv_id;
+                    out->tri = bits(a.w) * 3u;
+                    out->u = u;
+                    out->v = v;
+                }
+            }
+        }
+    } else if (type == ORN_NODE_SPHERE || type == ORN_NODE_MESH) {
+        float4 r2 = make_float4(c.x, c.y, c.z, e.x);
+        f3 to = mk(dot4(a, w.o.x, w.o.y, w.o.z, 1.0f), dot4(b, w.o.x, w.o.y, w.o.z, 1.0f),
+                   dot4(r2, w.o.x, w.o.y, w.o.z, 1.0f));
+        f3 td = mk(dot4(a, w.d.x, w.d.y, w.d.z, 0.0f), dot4(b, w.d.x, w.d.y, w.d.z, 0.0f),
+                   dot4(r2, w.d.x, w.d.y, w.d.z, 0.0f));
+        uint32_t mat = bits(e.y);
+        uint32_t inv_index = bits(e.z) * 2u;
+        if (type == ORN_NODE_SPHERE) {
+            if (COUNT) vc->sphere++;
+            float aa = td.x * td.x + td.y * td.y + td.z * td.z;
+            float half_b = dot(to, td);
+            float cc = (to.x * to.x + to.y * to.y + to.z * to.z) - 1.0f * 1.0f;
+            float disc = half_b * half_b - aa * cc;
+            float t = w.t_max;
+            if (!(disc < 0.0f)) {
+                float sq = sqrtf(disc);
+                t = (-half_b - sq) / aa;
+                if (t < t_min || w.t_max < t) {
+                    t = (-half_b + sq) / aa;
+                    if (t < t_min || w.t_max < t) t = w.t_max;
+                }
+            }
+            if (t < w.t_max) {
+                w.any = true;
+                w.t_max = t;
+                out->t = t;
+                out->material = mat;
+                out->type = ORN_NODE_SPHERE;
+                out->inv = inv_index;
+            }
+        } else {
+            if (COUNT) vc->mesh++;
+            w.in_blas = true;
+            w.blas_sp = w.sp;
+            w.inv_id = inv_index;
+            w.material = mat;
+            w.o = to;
+            w.d = td;
+            w.inv = safe_invdir(td);
+            w.oxinv = mul(neg(to), w.inv);
+            next = bits(e.w);
+            have_next = true;
+        }
+    }
+    if (!have_next) {
+        if (w.in_blas && w.sp == w.blas_sp) {
+            w.in_blas = false;
+            w.o = ro;
+            w.d = rd;
+            w.inv = safe_invdir(rd);
+            w.oxinv = mul(neg(ro), w.inv);
+        }
+        if (w.sp == 0) {
+            if (COUNT) vc->visits += w.visits;
+            return false;
+        }
+        next = stack.get(--w.sp);
+    }
+    w.node = next;
+    return true;
+}
+
+}  // namespace orn
