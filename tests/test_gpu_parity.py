@@ -49,6 +49,25 @@ def test_trace_rays_matches_reference_and_oracle(golden, golden_bvh, golden_rend
     assert np.array_equal(visits, ovisits)                              # per-ray node visits
 
 
+def test_trace_rays_exact_slab_fallback(golden_bvh, golden_renderer, oracle):
+    """Rays whose origins are NaN, infinite or beyond 1e30 take the
+    reference's own RT_MIN/RT_MAX slab form; all others the FMNMX form.
+    Both must give the reference's hits and visit counts."""
+    rs = np.random.default_rng(3)
+    rays = np.concatenate([rs.uniform(-3, 3, (512, 3)), rs.normal(size=(512, 3))], 1).astype(np.float32)
+    rays[0:8, 0] = np.nan
+    rays[8:16, 1] = np.inf
+    rays[16:24, 2] = -3e30
+    rays[24:32, 3:6] = 0.0                      # zero direction: safe_invdir clamps
+    rays[32:40, 3] = np.nan                     # NaN direction
+    rays[40:48, 0:3] = 1e29                     # large but below the guard
+    golden_renderer.set_state(make_state())
+    hits, visits = golden_renderer.trace_rays(rays)
+    ohits, ovisits = oracle.trace_rays(golden_bvh, rays)
+    assert np.array_equal(bits(hits), bits(ohits))
+    assert np.array_equal(visits, ovisits)
+
+
 def _golden_cases(golden):
     for c in golden["render_cases"]:
         name, spp, ci, depth, gamma, flip, base = str(c).split("|")

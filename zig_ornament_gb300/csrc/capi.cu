@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -34,6 +35,8 @@ struct orn_context {
     SceneDev scene{};
     uint32_t scene_textures_count = 0;
     uint32_t tlas_len = 0, blas_len = 0;
+    double world_extent = 0.0;        // largest |coordinate| of the TLAS bounds
+    double max_inverse_entry = 0.0;   // largest |entry| of the inverse transforms
 
     orn_state state{};
     orn_camera camera{};
@@ -109,8 +112,8 @@ int validate_blob(orn_context* ctx, const orn_scene_blob* b) {
         (b->uv_indices_len && !b->uv_indices) || (b->transforms_len && !b->transforms) ||
         (b->materials_len && !b->materials) || (b->textures_len && !b->textures))
         return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "blob array pointer is NULL with nonzero length");
-    if ((uint64_t)b->tlas_nodes_len + b->blas_nodes_len >= 0xFFFFFFFFull)
-        return fail(ctx, ORN_ERR_BAD_SCENE, "too many nodes");
+    if ((uint64_t)b->tlas_nodes_len + b->blas_nodes_len > 0x3FFFFFFFull)
+        return fail(ctx, ORN_ERR_BAD_SCENE, "too many nodes (at most 2^30)");
     for (uint32_t i = 0; i < b->tlas_nodes_len; ++i) {
         const orn_bvh_node& n = b->tlas_nodes[i];
         switch (n.node_type) {
@@ -176,6 +179,11 @@ void relayout_nodes(const orn_scene_blob* b, std::vector<float4>* out) {
     const uint32_t T = b->tlas_nodes_len, B = b->blas_nodes_len;
     out->assign((size_t)(T + B) * 4, make_float4(0, 0, 0, 0));
     auto u2f = [](uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; };
+    // reference to node `i` of the TLAS (blas=false) or BLAS, with its type
+    auto ref = [&](uint32_t i, bool blas) -> uint32_t {
+        const orn_bvh_node& c = blas ? b->blas_nodes[i] : b->tlas_nodes[i];
+        return ((blas ? T : 0u) + i) | (c.node_type << 30);
+    };
     auto put = [&](size_t idx, const orn_bvh_node& n, uint32_t child_offset) {
         float4* o = out->data() + idx * 4;
         const float* a = n.left_aabb_min_or_v0;
@@ -184,8 +192,8 @@ void relayout_nodes(const orn_scene_blob* b, std::vector<float4>* out) {
         const float* e = n.right_aabb_max_or_v3;
         switch (n.node_type) {
             case ORN_NODE_INTERNAL:
-                o[0] = make_float4(a[0], a[1], a[2], u2f(n.left_or_custom_id + child_offset));
-                o[1] = make_float4(bb[0], bb[1], bb[2], u2f(n.right_or_material_index + child_offset));
+                o[0] = make_float4(a[0], a[1], a[2], u2f(ref(n.left_or_custom_id, child_offset != 0)));
+                o[1] = make_float4(bb[0], bb[1], bb[2], u2f(ref(n.right_or_material_index, child_offset != 0)));
                 o[2] = make_float4(c[0], c[1], c[2], u2f(ORN_NODE_INTERNAL));
                 o[3] = make_float4(e[0], e[1], e[2], 0.0f);
                 break;
@@ -201,7 +209,7 @@ void relayout_nodes(const orn_scene_blob* b, std::vector<float4>* out) {
                 o[0] = make_float4(m[0], m[1], m[2], m[3]);
                 o[1] = make_float4(m[4], m[5], m[6], m[7]);
                 o[2] = make_float4(m[8], m[9], m[10], u2f(n.node_type));
-                uint32_t root = n.node_type == ORN_NODE_MESH ? n.left_or_custom_id + T : 0u;
+                uint32_t root = n.node_type == ORN_NODE_MESH ? ref(n.left_or_custom_id, true) : 0u;
                 o[3] = make_float4(m[11], u2f(n.right_or_material_index), u2f(n.transform_id), u2f(root));
                 break;
             }
@@ -264,6 +272,28 @@ orn_constant_params make_params(const orn_context* ctx, float current_iteration)
     cp.textures_count = ctx->scene_textures_count;
     cp.current_iteration = current_iteration;
     return cp;
+}
+
+// Whether every ray of a render satisfies the condition of the FMNMX slab
+// test (aabb_hit_fast: ray origin and node bounds finite and below 1e30 in
+// magnitude).  Render rays start at the camera (origin plus a lens offset)
+// or at a hit point, which lies inside the scene's world bounds; in a BLAS
+// the origin is that point mapped by an inverse transform.  With S the
+// largest world-space magnitude (scene bounds, camera origin plus lens) and
+// C the largest inverse-transform entry, object-space origins are bounded by
+// 4*C*(S+1).
+bool render_fast_slabs(const orn_context* ctx) {
+    if (ctx->scene.exact_slabs) return false;
+    const orn_camera& cam = ctx->camera;
+    double s = ctx->world_extent;
+    for (int i = 0; i < 3; ++i) {
+        double o = std::fabs((double)cam.origin[i]);
+        double l = 2.0 * (std::fabs((double)cam.u[i]) + std::fabs((double)cam.v[i])) * std::fabs((double)cam.lens_radius);
+        if (!std::isfinite(o) || !std::isfinite(l)) return false;
+        s = std::max(s, o + l);
+    }
+    if (!(s < 1e29)) return false;
+    return 4.0 * ctx->max_inverse_entry * (s + 1.0) < 1e29;
 }
 
 constexpr int kWfRing = 16;
@@ -329,6 +359,7 @@ int render_wavefront_sweep(orn_context* ctx, const orn_constant_params& cp, uint
     ORN_CUDA(ctx, cudaMemsetAsync(w.pixel_counter, 0, 4 * sizeof(uint32_t), ctx->stream));
     ORN_CUDA(ctx, cudaMemsetAsync(w.qstat, 0, 16 * sizeof(uint32_t), ctx->stream));
     const int sem = (int)ctx->state.semantics;
+    const bool fast = render_fast_slabs(ctx);
     // Upper bound on iterations: every ray of every sample of every pixel
     // (protects against a logic error turning into an endless host loop).
     const uint64_t max_iter = (uint64_t)spp * (ctx->state.depth + 1) *
@@ -346,7 +377,7 @@ int render_wavefront_sweep(orn_context* ctx, const orn_constant_params& cp, uint
         ORN_CUDA(ctx, cudaMemcpyAsync(ctx->wf_host_stat + 2 * r, w.qstat + 4 * (iter & 3), 2 * sizeof(uint32_t),
                                       cudaMemcpyDeviceToHost, ctx->stream));
         ORN_CUDA(ctx, cudaEventRecord(ctx->wf_events[r], ctx->stream));
-        ORN_CUDA(ctx, orn::launch_wf_extend(w, iter, ctx->counters_enabled, ctx->stream));
+        ORN_CUDA(ctx, orn::launch_wf_extend(w, iter, ctx->counters_enabled, fast, ctx->stream));
         ctx->launches += 2;
     }
     return ORN_OK;
@@ -448,6 +479,45 @@ int orn_create(const orn_scene_blob* blob, int device, orn_context** out) {
         ctx->scene.nodes = d_nodes;
         ctx->scene.tlas_len = blob->tlas_nodes_len;
         ctx->scene.node_count = blob->tlas_nodes_len + blob->blas_nodes_len;
+        ctx->scene.root_ref = (blob->tlas_nodes_len - 1) |
+                              (blob->tlas_nodes[blob->tlas_nodes_len - 1].node_type << 30);
+        // The FMNMX slab test needs every internal-node bound finite and
+        // below 1e30 in magnitude (pt_device.cuh, aabb_hit_fast).
+        bool huge = false;
+        auto check_bounds = [&](const orn_bvh_node* nodes, uint32_t n) {
+            for (uint32_t i = 0; i < n && !huge; ++i) {
+                if (nodes[i].node_type != ORN_NODE_INTERNAL) continue;
+                const float* f[4] = {nodes[i].left_aabb_min_or_v0, nodes[i].left_aabb_max_or_v1,
+                                     nodes[i].right_aabb_min_or_v2, nodes[i].right_aabb_max_or_v3};
+                for (int k = 0; k < 4; ++k)
+                    for (int j = 0; j < 3; ++j)
+                        if (!(std::fabs(f[k][j]) < 1e30f)) huge = true;
+            }
+        };
+        check_bounds(blob->tlas_nodes, blob->tlas_nodes_len);
+        check_bounds(blob->blas_nodes, blob->blas_nodes_len);
+        for (uint32_t i = 0; i < blob->tlas_nodes_len; ++i) {
+            const orn_bvh_node& n = blob->tlas_nodes[i];
+            const float* f[4] = {n.left_aabb_min_or_v0, n.left_aabb_max_or_v1, n.right_aabb_min_or_v2,
+                                 n.right_aabb_max_or_v3};
+            int boxes = n.node_type == ORN_NODE_INTERNAL ? 4 : 2;
+            for (int k = 0; k < boxes; ++k)
+                for (int j = 0; j < 3; ++j) {
+                    double v = std::fabs((double)f[k][j]);
+                    if (!std::isfinite(v)) huge = true;
+                    else ctx->world_extent = std::max(ctx->world_extent, v);
+                }
+        }
+        for (uint32_t t = 0; t < blob->transforms_len; t += 2)
+            for (int j = 0; j < 16; ++j) {
+                double v = std::fabs((double)blob->transforms[(size_t)t * 16 + j]);
+                if (!std::isfinite(v)) huge = true;
+                else ctx->max_inverse_entry = std::max(ctx->max_inverse_entry, v);
+            }
+        ctx->scene.exact_slabs = huge ? 1u : 0u;
+#ifdef ORN_FORCE_EXACT_SLABS
+        ctx->scene.exact_slabs = 1u;
+#endif
         ctx->scene.xforms = d_x;
         ctx->scene.normals = d_n;
         ctx->scene.normal_indices = d_ni;
@@ -583,7 +653,7 @@ int orn_render(orn_context* ctx) {
             if (st) return st;
         } else {
             ORN_CUDA(ctx, orn::launch_mega(p, (int)ctx->state.semantics, orn::MATH_PORTABLE,
-                                           ctx->counters_enabled, ctx->stream));
+                                           ctx->counters_enabled, render_fast_slabs(ctx), ctx->stream));
             ctx->launches++;
         }
         done += n;

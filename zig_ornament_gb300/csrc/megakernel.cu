@@ -25,7 +25,7 @@ enum LaneMode { LANE_IDLE = 0, LANE_TRAVERSE = 1, LANE_SHADE = 2, LANE_DONE = 3 
 // 32 at a time from p.work_counter; each pixel runs its p.spp passes with the
 // accumulation and RNG state in registers, then writes them back (and the
 // post-processed framebuffer value when p.do_post).
-template <int SEM, int MATH, bool COUNT>
+template <int SEM, int MATH, bool COUNT, bool FAST>
 __global__ void __launch_bounds__(kMegaBlock)
 mega_kernel(RenderLaunch p) {
     __shared__ uint32_t sstack[kSmemStack * kMegaBlock];
@@ -105,8 +105,13 @@ mega_kernel(RenderLaunch p) {
             break;
 
         if (mode == LANE_TRAVERSE) {
-            if (!walker_step<COUNT, kSmemStack>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon, &h, stack, &vc, &err))
-                mode = LANE_SHADE;
+#pragma unroll 1
+            for (int s = 0; s < kStepsPerIteration; ++s) {
+                if (!walker_step<COUNT, kSmemStack, FAST>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon, &h, stack, &vc, &err)) {
+                    mode = LANE_SHADE;
+                    break;
+                }
+            }
         }
 
         const unsigned ready = __ballot_sync(kFull, mode == LANE_SHADE);
@@ -202,14 +207,14 @@ __global__ void post_kernel(const float4* __restrict__ acc, float4* __restrict__
 // ---- host-side launchers -----------------------------------------------------
 // Persistent grid: as many blocks as fit on the device at once (never more
 // than the pixels need).
-template <int SEM, int MATH, bool COUNT>
+template <int SEM, int MATH, bool COUNT, bool FAST>
 static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
     static int blocks_per_sm = 0, sms = 0;
     if (blocks_per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT>, kMegaBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST>, kMegaBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     uint32_t need = (p.pixel_count + kMegaBlock - 1) / kMegaBlock;
@@ -217,22 +222,24 @@ static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
     if (need < grid) grid = need;
     cudaError_t e = cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    mega_kernel<SEM, MATH, COUNT><<<grid, kMegaBlock, 0, s>>>(p);
+    mega_kernel<SEM, MATH, COUNT, FAST><<<grid, kMegaBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 
-template <int SEM, int MATH>
-static cudaError_t launch_mega_t(const RenderLaunch& p, bool count, cudaStream_t s) {
-    return count ? launch_mega_tt<SEM, MATH, true>(p, s) : launch_mega_tt<SEM, MATH, false>(p, s);
+template <int SEM>
+static cudaError_t launch_mega_t(const RenderLaunch& p, bool count, bool fast, cudaStream_t s) {
+    if (fast) return count ? launch_mega_tt<SEM, MATH_PORTABLE, true, true>(p, s)
+                           : launch_mega_tt<SEM, MATH_PORTABLE, false, true>(p, s);
+    return count ? launch_mega_tt<SEM, MATH_PORTABLE, true, false>(p, s)
+                 : launch_mega_tt<SEM, MATH_PORTABLE, false, false>(p, s);
 }
 
-cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, cudaStream_t s) {
-    if (semantics == SEM_WGSL) {
-        return math == MATH_DEVICE ? launch_mega_t<SEM_WGSL, MATH_DEVICE>(p, count, s)
-                                   : launch_mega_t<SEM_WGSL, MATH_PORTABLE>(p, count, s);
-    }
-    return math == MATH_DEVICE ? launch_mega_t<SEM_HIP, MATH_DEVICE>(p, count, s)
-                               : launch_mega_t<SEM_HIP, MATH_PORTABLE>(p, count, s);
+// The render kernels always use the portable transcendentals (bit-exact
+// with the CPU restatement); `math` is accepted for the launch interface.
+cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, bool fast, cudaStream_t s) {
+    (void)math;
+    return semantics == SEM_WGSL ? launch_mega_t<SEM_WGSL>(p, count, fast, s)
+                                 : launch_mega_t<SEM_HIP>(p, count, fast, s);
 }
 
 cudaError_t launch_trace_rays(const SceneDev& sc, float t_min, const float* rays, size_t count,

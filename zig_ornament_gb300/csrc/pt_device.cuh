@@ -122,6 +122,28 @@ __device__ __forceinline__ bool aabb_hit(float4 mn, float4 mx, f3 inv, f3 oxinv,
     return min_t <= max_t;
 }
 
+// The same slab test with fminf/fmaxf (one FMNMX each) in place of the
+// reference's RT_MIN/RT_MAX (a compare and a select each).  For inputs
+// without NaN the two forms return numerically equal values (they can only
+// disagree on the sign of a zero result), and `min_t <= max_t` does not see
+// zero signs, so the decision is identical.  The slab values are NaN-free
+// whenever the ray origin and the box bounds are finite with magnitude below
+// 1e30: |invdir| <= 1e5 by construction (safe_invdir), so every product and
+// sum stays finite.  Callers use this form only under that condition
+// (Walker::fast_slabs, SceneDev::exact_slabs).
+__device__ __forceinline__ bool aabb_hit_fast(float4 mn, float4 mx, f3 inv, f3 oxinv, float t_min, float t_max) {
+    float fx = mx.x * inv.x + oxinv.x, fy = mx.y * inv.y + oxinv.y, fz = mx.z * inv.z + oxinv.z;
+    float nx = mn.x * inv.x + oxinv.x, ny = mn.y * inv.y + oxinv.y, nz = mn.z * inv.z + oxinv.z;
+    float max_t = fminf(fminf(fminf(fmaxf(fx, nx), fmaxf(fy, ny)), fmaxf(fz, nz)), t_max);
+    float min_t = fmaxf(fmaxf(fmaxf(fminf(fx, nx), fminf(fy, ny)), fminf(fz, nz)), t_min);
+    return min_t <= max_t;
+}
+
+// True when every component of o is finite with magnitude below 1e30.
+__device__ __forceinline__ bool slab_safe(f3 o) {
+    return fabsf(o.x) < 1e30f && fabsf(o.y) < 1e30f && fabsf(o.z) < 1e30f;
+}
+
 struct HitRec {
     float t;
     uint32_t material;
@@ -165,27 +187,35 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
     stack.sstack = sstack;
     stack.sstride = sstride;
     int sp = 0;
-    uint32_t node = sc.tlas_len - 1;
+    uint32_t node = sc.root_ref;
     bool in_blas = false;
     int blas_sp = 0;
     f3 o = ro, d = rd;
     f3 inv = safe_invdir(d);
     f3 oxinv = mul(neg(o), inv);
     const f3 winv = inv, woxinv = oxinv;
+    const bool wfast = !sc.exact_slabs && slab_safe(ro);
+    bool fast = wfast;
     uint32_t material = 0, inv_id = 0;
     bool any = false;
     uint32_t visits = 0;
     for (;;) {
         if (++visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; return false; }
-        const float4* np = sc.nodes + 4 * (size_t)node;
+        const float4* np = sc.nodes + 4 * (size_t)(node & kRefIndexMask);
         float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
         uint32_t type = bits(c.w);
         bool have_next = false;
         uint32_t next = 0;
         if (type == ORN_NODE_INTERNAL) {
             if (COUNT) vc->internal++;
-            bool hl = aabb_hit(a, b, inv, oxinv, t_min, t_max);
-            bool hr = aabb_hit(c, e, inv, oxinv, t_min, t_max);
+            bool hl, hr;
+            if (fast) {
+                hl = aabb_hit_fast(a, b, inv, oxinv, t_min, t_max);
+                hr = aabb_hit_fast(c, e, inv, oxinv, t_min, t_max);
+            } else {
+                hl = aabb_hit(a, b, inv, oxinv, t_min, t_max);
+                hr = aabb_hit(c, e, inv, oxinv, t_min, t_max);
+            }
             if (hr) {
                 next = bits(b.w);
                 have_next = true;
@@ -267,6 +297,7 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
                 d = td;
                 inv = safe_invdir(d);
                 oxinv = mul(neg(o), inv);
+                fast = !sc.exact_slabs && slab_safe(to);
                 next = bits(e.w);
                 have_next = true;
             }
@@ -278,6 +309,7 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
                 d = rd;
                 inv = winv;
                 oxinv = woxinv;
+                fast = wfast;
             }
             if (sp == 0) break;
             next = stack.get(--sp);

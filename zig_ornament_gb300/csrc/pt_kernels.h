@@ -34,6 +34,12 @@ struct RenderLaunch {
 #define ORN_SHADE_THRESHOLD 8
 #endif
 constexpr int kShadeThreshold = ORN_SHADE_THRESHOLD;
+// BVH node visits a traversing lane makes per pass of the megakernel's loop
+// (amortises the loop's ballots).
+#ifndef ORN_STEPS_PER_ITERATION
+#define ORN_STEPS_PER_ITERATION 8
+#endif
+constexpr int kStepsPerIteration = ORN_STEPS_PER_ITERATION;
 
 // Arguments of one wavefront iteration (wavefront.cu).  Path slots are
 // structure-of-arrays; qstat holds per-iteration [queue count, slots waiting
@@ -65,12 +71,15 @@ struct WaveLaunch {
     int fetch_threshold;
 };
 
-constexpr int kFetchThreshold = 16;
+#ifndef ORN_FETCH_THRESHOLD
+#define ORN_FETCH_THRESHOLD 16
+#endif
+constexpr int kFetchThreshold = ORN_FETCH_THRESHOLD;
 
-cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, cudaStream_t s);
+cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, bool fast, cudaStream_t s);
 cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, int math, bool count,
                             cudaStream_t s);
-cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, cudaStream_t s);
+cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, bool fast, cudaStream_t s);
 cudaError_t launch_trace_rays(const SceneDev& sc, float t_min, const float* rays, size_t count,
                               orn_hit* hits, uint32_t* visits, uint32_t* error, cudaStream_t s);
 cudaError_t launch_seed_rng(uint32_t* rng, uint32_t n, cudaStream_t s);

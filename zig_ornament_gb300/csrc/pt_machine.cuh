@@ -24,7 +24,8 @@
 namespace orn {
 
 // Traversal state of one ray, advanced one node per step
-// (bvh.hip.h:145-276 visit order; see trace_ray).
+// (bvh.hip.h:145-276 visit order; see trace_ray).  `node` is a typed node
+// reference (pt_scene.h).
 struct Walker {
     uint32_t node;
     int sp;
@@ -32,13 +33,16 @@ struct Walker {
     bool in_blas;
     bool any;
     f3 o, d, inv, oxinv;
+#ifndef ORN_RECOMPUTE_WORLD_INV
+    f3 winv, woxinv;   // world-space values, restored on BLAS exit
+#endif
     float t_max;
     uint32_t material, inv_id;
     uint32_t visits;
 };
 
 __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 ro, f3 rd) {
-    w.node = sc.tlas_len - 1;
+    w.node = sc.root_ref;
     w.sp = 0;
     w.blas_sp = 0;
     w.in_blas = false;
@@ -47,29 +51,43 @@ __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 r
     w.d = rd;
     w.inv = safe_invdir(rd);
     w.oxinv = mul(neg(ro), w.inv);
+#ifndef ORN_RECOMPUTE_WORLD_INV
+    w.winv = w.inv;
+    w.woxinv = w.oxinv;
+#endif
     w.t_max = (float)3.40282e+38;
     w.material = 0;
     w.inv_id = 0;
     w.visits = 0;
 }
 
-// Visits the current node; returns false when the traversal has finished.
-// The world-space inverse direction is recomputed on BLAS exit (the same
-// operations give the same bits) instead of being kept in registers.
-template <bool COUNT, int SS>
+// Visits the lane's current node; returns false when the traversal has
+// finished.  The three node kinds are separate branches; a warp runs each
+// branch that any of its lanes needs (grouping lanes by node kind measured
+// slower on sm_103a: the lanes kept waiting cost more than the divergence).
+// FAST selects the FMNMX slab test (aabb_hit_fast); the host decides per
+// render whether every ray of the render satisfies its condition
+// (render_fast_slabs in capi.cu).
+template <bool COUNT, int SS, bool FAST>
 __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro, f3 rd, float t_min,
                                             HitRec* out, TravStack<SS>& stack, VisitCount* vc,
                                             uint32_t* err) {
     if (++w.visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; w.any = false; return false; }
-    const float4* np = sc.nodes + 4 * (size_t)w.node;
-    float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
-    uint32_t type = bits(c.w);
+    const uint32_t type = w.node >> 30;
+    const float4* np = sc.nodes + 4 * (size_t)(w.node & kRefIndexMask);
     bool have_next = false;
     uint32_t next = 0;
     if (type == ORN_NODE_INTERNAL) {
         if (COUNT) vc->internal++;
-        bool hl = aabb_hit(a, b, w.inv, w.oxinv, t_min, w.t_max);
-        bool hr = aabb_hit(c, e, w.inv, w.oxinv, t_min, w.t_max);
+        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
+        bool hl, hr;
+        if (FAST) {
+            hl = aabb_hit_fast(a, b, w.inv, w.oxinv, t_min, w.t_max);
+            hr = aabb_hit_fast(c, e, w.inv, w.oxinv, t_min, w.t_max);
+        } else {
+            hl = aabb_hit(a, b, w.inv, w.oxinv, t_min, w.t_max);
+            hr = aabb_hit(c, e, w.inv, w.oxinv, t_min, w.t_max);
+        }
         if (hr) {
             next = bits(b.w);
             have_next = true;
@@ -83,6 +101,7 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
         }
     } else if (type == ORN_NODE_TRIANGLE) {
         if (COUNT) vc->tri++;
+        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2);
         f3 v1 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
         f3 s1 = cross(w.d, e2);
         float det = dot(s1, e1);
@@ -107,7 +126,8 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
                 }
             }
         }
-    } else if (type == ORN_NODE_SPHERE || type == ORN_NODE_MESH) {
+    } else {
+        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
         float4 r2 = make_float4(c.x, c.y, c.z, e.x);
         f3 to = mk(dot4(a, w.o.x, w.o.y, w.o.z, 1.0f), dot4(b, w.o.x, w.o.y, w.o.z, 1.0f),
                    dot4(r2, w.o.x, w.o.y, w.o.z, 1.0f));
@@ -157,8 +177,13 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
             w.in_blas = false;
             w.o = ro;
             w.d = rd;
+#ifdef ORN_RECOMPUTE_WORLD_INV
             w.inv = safe_invdir(rd);
             w.oxinv = mul(neg(ro), w.inv);
+#else
+            w.inv = w.winv;
+            w.oxinv = w.woxinv;
+#endif
         }
         if (w.sp == 0) {
             if (COUNT) vc->visits += w.visits;

@@ -11,6 +11,11 @@
 //   mesh      as sphere with type=2 and e.w = BLAS root id
 // (BvhNode, src/gpu_structs.zig:22-31, carries the same information; the
 // leaf's own AABB, unused by traversal, is replaced by the transform rows.)
+//
+// Node references (child ids, the BLAS root of a mesh leaf, stack entries)
+// carry the referenced node's type in their top two bits:
+// ref = index | type << 30.  A warp therefore knows the type of every lane's
+// next node before loading it and can process one node type at a time.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -22,6 +27,7 @@ enum { SEM_HIP = 0, SEM_WGSL = 1 };          // enum orn_semantics
 enum { MATH_PORTABLE = 0, MATH_DEVICE = 1 };  // transcendental implementation
 // Error bits written to the context's device error word.
 enum { ERR_STACK = 1u, ERR_VISITS = 2u };
+constexpr uint32_t kRefIndexMask = 0x3FFFFFFFu;
 
 struct TexDesc {
     const unsigned char* data;
@@ -32,6 +38,8 @@ struct SceneDev {
     const float4* nodes;        // 4 float4 per node, TLAS then BLAS
     uint32_t tlas_len;
     uint32_t node_count;
+    uint32_t root_ref;          // reference of the TLAS root
+    uint32_t exact_slabs;       // 1: some node bound is non-finite or >= 1e30 in magnitude
     const float4* xforms;       // 4 float4 per matrix, blob transforms as given
     const float4* normals;
     const uint32_t* normal_indices;

@@ -180,7 +180,7 @@ wf_logic(WaveLaunch p, uint32_t iter) {
     }
 }
 
-template <bool COUNT>
+template <bool COUNT, bool FAST>
 __global__ void __launch_bounds__(kMegaBlock)
 wf_extend(WaveLaunch p, uint32_t iter) {
     __shared__ uint32_t sstack[kSmemStack * kMegaBlock];
@@ -224,7 +224,7 @@ wf_extend(WaveLaunch p, uint32_t iter) {
         if (drained && __ballot_sync(kFull, slot != 0xffffffffu) == 0u) break;
         if (slot != 0xffffffffu) {
             uint32_t e0 = err;
-            if (!walker_step<COUNT, kSmemStack>(w, p.scene, ro, rd, t_min, &h, stack, &vc, &err)) {
+            if (!walker_step<COUNT, kSmemStack, FAST>(w, p.scene, ro, rd, t_min, &h, stack, &vc, &err)) {
                 uint32_t flag = (err != e0) ? 2u : (w.any ? 1u : 0u);
                 p.hit[2 * slot] = make_float4(h.t, __uint_as_float(h.material), __uint_as_float(h.type),
                                               __uint_as_float(h.inv));
@@ -261,23 +261,26 @@ cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, i
                                : logic_t<SEM_HIP, MATH_PORTABLE>(p, iter, count, s);
 }
 
-cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, cudaStream_t s) {
-    static int blocks_per_sm[2] = {0, 0}, sms = 0;
-    int c = count ? 1 : 0;
-    if (blocks_per_sm[c] == 0) {
+template <bool COUNT, bool FAST>
+static cudaError_t extend_t(const WaveLaunch& p, uint32_t iter, cudaStream_t s) {
+    static int blocks_per_sm = 0, sms = 0;
+    if (blocks_per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (count) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[c], wf_extend<true>, kMegaBlock, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[c], wf_extend<false>, kMegaBlock, 0);
-        if (blocks_per_sm[c] < 1) blocks_per_sm[c] = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, wf_extend<COUNT, FAST>, kMegaBlock, 0);
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
-    uint32_t grid = (uint32_t)(blocks_per_sm[c] * sms);
+    uint32_t grid = (uint32_t)(blocks_per_sm * sms);
     uint32_t need = (p.slots + kMegaBlock - 1) / kMegaBlock;
     if (need < grid) grid = need;
-    if (count) wf_extend<true><<<grid, kMegaBlock, 0, s>>>(p, iter);
-    else wf_extend<false><<<grid, kMegaBlock, 0, s>>>(p, iter);
+    wf_extend<COUNT, FAST><<<grid, kMegaBlock, 0, s>>>(p, iter);
     return cudaGetLastError();
+}
+
+cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, bool fast, cudaStream_t s) {
+    if (fast) return count ? extend_t<true, true>(p, iter, s) : extend_t<false, true>(p, iter, s);
+    return count ? extend_t<true, false>(p, iter, s) : extend_t<false, false>(p, iter, s);
 }
 
 }  // namespace orn
