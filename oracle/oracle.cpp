@@ -545,12 +545,13 @@ int oracle_trace_rays(const orn_scene_blob* blob, float ray_cast_epsilon, const 
 // one thread, which gives the same per-pixel RNG stream and accumulation
 // order as one launch per pass.  acc/fb: pixel_count float4; rng: u32 each.
 // acc64 (optional): FP64 accumulation of the same samples (sum only).
-// Pixels [pixel_begin, pixel_end) are rendered (a bounded sample of the
-// frame); post-processing covers the same range.
+// Pixels pixel_begin, pixel_begin + pixel_stride, ... below pixel_end are
+// rendered (a bounded sample of the frame); post-processing covers the same
+// pixels.
 int oracle_render(const orn_scene_blob* blob, const orn_constant_params* cp, uint32_t spp,
                   float ci_start, int semantics, int portable_math, float* acc, uint32_t* rng,
                   float* fb, double* acc64, uint32_t pixel_begin, uint32_t pixel_end,
-                  int threads, uint64_t* counters) {
+                  uint32_t pixel_stride, int threads, uint64_t* counters) {
     if (!blob || !cp || !acc || !rng || !fb || spp == 0) return ORN_ERR_INVALID_ARGUMENT;
     if (blob->tlas_nodes_len == 0) return ORN_ERR_EMPTY_SCENE;
     Scene s;
@@ -558,6 +559,8 @@ int oracle_render(const orn_scene_blob* blob, const orn_constant_params* cp, uin
     const uint32_t W = cp->width, H = cp->height;
     const uint32_t pixel_count = W * H;
     if (pixel_end > pixel_count) pixel_end = pixel_count;
+    if (pixel_stride == 0) pixel_stride = 1;
+    const uint32_t n_px = pixel_end > pixel_begin ? (pixel_end - pixel_begin + pixel_stride - 1) / pixel_stride : 0;
     if (threads <= 0) threads = omp_get_max_threads();
     Params p;
     p.cp = *cp;
@@ -570,7 +573,8 @@ int oracle_render(const orn_scene_blob* blob, const orn_constant_params* cp, uin
     {
         Counters local{};
 #pragma omp for schedule(dynamic, 64)
-        for (uint32_t gid = pixel_begin; gid < pixel_end; ++gid) {
+        for (uint32_t ip = 0; ip < n_px; ++ip) {
+            const uint32_t gid = pixel_begin + ip * pixel_stride;
             uint32_t x = gid % W, y = gid / W;
             Rng r{rng[gid]};
             V4 a = {acc[4 * gid], acc[4 * gid + 1], acc[4 * gid + 2], acc[4 * gid + 3]};

@@ -31,7 +31,7 @@ class Oracle:
         self.lib.oracle_trace_rays.argtypes = [_P, C.c_float, _P, C.c_size_t, _P, _P, C.c_int]
         self.lib.oracle_render.restype = C.c_int
         self.lib.oracle_render.argtypes = [_P, _P, C.c_uint32, C.c_float, C.c_int, C.c_int, _P, _P, _P, _P,
-                                           C.c_uint32, C.c_uint32, C.c_int, _P]
+                                           C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, _P]
         for fn in ("oracle_pm_eval", "oracle_libm_eval"):
             getattr(self.lib, fn).restype = None
             getattr(self.lib, fn).argtypes = [C.c_int, _P, _P, _P, _P, C.c_size_t]
@@ -48,7 +48,7 @@ class Oracle:
         return hits, visits
 
     def render(self, bvh, cp, spp, ci_start=1.0, acc=None, rng=None, semantics=0, portable_math=True,
-               acc64=None, pixel_range=None, threads=0, counters=False):
+               acc64=None, pixel_range=None, pixel_stride=1, threads=0, counters=False):
         """Returns (acc, rng, fb, counters).  acc/rng default to a fresh
         target (zeros, RNG seeded with the pixel index)."""
         n = cp.width * cp.height
@@ -59,7 +59,8 @@ class Oracle:
         lo, hi = pixel_range if pixel_range else (0, n)
         blob, keep = bvh.blob()
         st = self.lib.oracle_render(C.byref(blob), C.byref(cp), spp, ci_start, semantics, 1 if portable_math else 0,
-                                    _ptr(acc), _ptr(rng), _ptr(fb), _ptr(acc64), lo, hi, threads, _ptr(cnt))
+                                    _ptr(acc), _ptr(rng), _ptr(fb), _ptr(acc64), lo, hi, pixel_stride, threads,
+                                    _ptr(cnt))
         if st != 0:
             raise RuntimeError(f"oracle_render failed with status {st}")
         return acc, rng, fb, cnt

@@ -26,7 +26,7 @@ enum LaneMode { LANE_IDLE = 0, LANE_TRAVERSE = 1, LANE_SHADE = 2, LANE_DONE = 3 
 // accumulation and RNG state in registers, then writes them back (and the
 // post-processed framebuffer value when p.do_post).
 template <int SEM, int MATH, bool COUNT, bool FAST>
-__global__ void __launch_bounds__(kMegaBlock)
+__global__ void __launch_bounds__(kMegaBlock, kMegaMinBlocks)
 mega_kernel(RenderLaunch p) {
     __shared__ uint32_t sstack[kSmemStack * kMegaBlock];
     TravStack<kSmemStack> stack;

@@ -63,6 +63,21 @@ __device__ __forceinline__ float dot4(float4 r, float x, float y, float z, float
 __device__ __forceinline__ uint32_t bits(float f) { return __float_as_uint(f); }
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
+// Two float4 with one 256-bit read-only load (sm_100+).  A lane's request
+// then fills a whole 32-byte L1 sector instead of half of one; nodes are
+// 64-byte aligned.
+__device__ __forceinline__ void ldg8(const float4* p, float4* lo, float4* hi) {
+#ifdef ORN_NODE_LOAD_V4
+    *lo = __ldg(p);
+    *hi = __ldg(p + 1);
+    return;
+#endif
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(lo->x), "=f"(lo->y), "=f"(lo->z), "=f"(lo->w), "=f"(hi->x), "=f"(hi->y), "=f"(hi->z),
+                   "=f"(hi->w)
+                 : "l"(p));
+}
+
 template <int MATH> struct DevMath;
 template <> struct DevMath<MATH_PORTABLE> {
     __device__ static float pow(float a, float b) { return pm_powf(a, b); }

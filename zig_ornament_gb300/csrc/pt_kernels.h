@@ -12,7 +12,12 @@
 namespace orn {
 
 constexpr int kMegaBlock = 128;
-constexpr int kSmemStack = 32;   // traversal-stack entries per thread kept in shared memory
+constexpr int kSmemStack = 32;
+// Resident blocks per SM the megakernel is compiled for (register cap).
+#ifndef ORN_MEGA_MIN_BLOCKS
+#define ORN_MEGA_MIN_BLOCKS 6
+#endif
+constexpr int kMegaMinBlocks = ORN_MEGA_MIN_BLOCKS;   // traversal-stack entries per thread kept in shared memory
 
 // Arguments of one megakernel launch (passed by value).
 struct RenderLaunch {

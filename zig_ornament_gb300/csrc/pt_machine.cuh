@@ -79,7 +79,9 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
     uint32_t next = 0;
     if (type == ORN_NODE_INTERNAL) {
         if (COUNT) vc->internal++;
-        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
+        float4 a, b, c, e;
+        ldg8(np, &a, &b);
+        ldg8(np + 2, &c, &e);
         bool hl, hr;
         if (FAST) {
             hl = aabb_hit_fast(a, b, w.inv, w.oxinv, t_min, w.t_max);
@@ -101,7 +103,10 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
         }
     } else if (type == ORN_NODE_TRIANGLE) {
         if (COUNT) vc->tri++;
-        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2);
+        float4 a, b, c, e;
+        ldg8(np, &a, &b);
+        ldg8(np + 2, &c, &e);
+        (void)e;
         f3 v1 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
         f3 s1 = cross(w.d, e2);
         float det = dot(s1, e1);
@@ -127,7 +132,9 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
             }
         }
     } else {
-        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
+        float4 a, b, c, e;
+        ldg8(np, &a, &b);
+        ldg8(np + 2, &c, &e);
         float4 r2 = make_float4(c.x, c.y, c.z, e.x);
         f3 to = mk(dot4(a, w.o.x, w.o.y, w.o.z, 1.0f), dot4(b, w.o.x, w.o.y, w.o.z, 1.0f),
                    dot4(r2, w.o.x, w.o.y, w.o.z, 1.0f));
