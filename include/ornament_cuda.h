@@ -277,6 +277,38 @@ int orn_get_stream(const orn_context* ctx, void** stream);
 /* Number of kernel launches the context has issued since creation. */
 int orn_launch_count(const orn_context* ctx, uint64_t* launches);
 
+/* ---- rendering without allocation -----------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they render — a frame loop that must never call cudaMalloc
+ * (an allocation can synchronise the device and stall the frame), or a host
+ * that gives the renderer a fixed memory budget — this renders with the
+ * wavefront kernels into device buffers the caller owns and allocates
+ * nothing: its working memory is a fixed array inside the library, sized for
+ * ORN_NOALLOC_MAX_PIXELS pixels (about 15 MiB, held on every GPU that loads
+ * the library until the process exits).
+ *
+ * `ctx` supplies the scene (uploaded by orn_create) and the semantics;
+ * `params` is the complete ConstantParams of the first pass (camera,
+ * resolution, depth, flip_y, inverted_gamma, epsilon, textures_count and
+ * current_iteration, as PathTracer.update() would upload it); `spp` passes
+ * run with current_iteration, current_iteration + 1, …, then
+ * post-processing.  `accumulation` (float4 per pixel) and `rng_state` (u32
+ * per pixel) are device buffers read and updated in place (seed a fresh
+ * render with rng_state[i] = i); `framebuffer` (float4 per pixel) is a
+ * device buffer written.  Work is queued on `stream` (a cudaStream_t; NULL
+ * is the default stream) and the call returns without waiting; device-side
+ * errors surface at the context's next orn_synchronize.  Results are
+ * bit-identical to orn_render with the same state.
+ *
+ * Returns ORN_ERR_INVALID_ARGUMENT when width * height exceeds
+ * ORN_NOALLOC_MAX_PIXELS or a pointer is NULL.  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls whose GPU work overlaps (other streams, other threads) race. */
+#define ORN_NOALLOC_MAX_PIXELS 131072u
+int orn_render_noalloc(const orn_context* ctx, const orn_constant_params* params, uint32_t spp,
+                       float* accumulation, uint32_t* rng_state, float* framebuffer, void* stream);
+
 /* ---- errors ------------------------------------------------------------- */
 const char* orn_last_error(const orn_context* ctx);
 const char* orn_status_string(int status);

@@ -27,6 +27,7 @@ TEXEL_RGBA8, TEXEL_RGBA16F = 0, 1
 SEMANTICS_HIP, SEMANTICS_WGSL = 0, 1
 KERNEL_MEGA, KERNEL_WAVEFRONT = 0, 1
 COUNTER_COUNT = 10
+NOALLOC_MAX_PIXELS = 131072
 COUNTER_NAMES = ["samples", "rays", "visits", "internal", "sphere_leaf", "mesh_entry", "triangle",
                  "sphere_hits", "mesh_hits", "textured_hits"]
 
@@ -158,6 +159,7 @@ FUNCTIONS = {
     "orn_last_render_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "orn_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "orn_launch_count": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "orn_render_noalloc": (C.c_int, [_P, C.POINTER(ConstantParams), C.c_uint32, _P, _P, _P, _P]),
     "orn_last_error": (C.c_char_p, [_P]),
     "orn_status_string": (C.c_char_p, [C.c_int]),
     "orn_abi_version": (C.c_uint32, []),

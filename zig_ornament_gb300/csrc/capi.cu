@@ -385,6 +385,34 @@ int render_wavefront_sweep(orn_context* ctx, const orn_constant_params& cp, uint
 
 }  // namespace
 
+namespace orn {
+
+// For orn_render_noalloc (noalloc.cu): the device-resident scene of a
+// context and what a render with `camera` needs to launch the wavefront
+// (the FMNMX slab condition is render_fast_slabs' check for that camera).
+const SceneDev* context_scene(const orn_context* ctx, int* device, uint32_t* semantics, uint32_t** error_word,
+                              bool* fast_slabs, const orn_camera* camera) {
+    if (!ctx || !camera) return nullptr;
+    *device = ctx->device;
+    *semantics = ctx->state.semantics;
+    *error_word = ctx->d_error;
+    bool fast = !ctx->scene.exact_slabs;
+    double s = ctx->world_extent;
+    for (int i = 0; i < 3 && fast; ++i) {
+        double o = std::fabs((double)camera->origin[i]);
+        double l = 2.0 * (std::fabs((double)camera->u[i]) + std::fabs((double)camera->v[i])) *
+                   std::fabs((double)camera->lens_radius);
+        if (!std::isfinite(o) || !std::isfinite(l)) fast = false;
+        else s = std::max(s, o + l);
+    }
+    if (fast && !(s < 1e29)) fast = false;
+    if (fast && !(4.0 * ctx->max_inverse_entry * (s + 1.0) < 1e29)) fast = false;
+    *fast_slabs = fast;
+    return &ctx->scene;
+}
+
+}  // namespace orn
+
 extern "C" {
 
 uint32_t orn_abi_version(void) { return ORN_ABI_VERSION; }

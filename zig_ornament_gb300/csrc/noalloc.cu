@@ -1,0 +1,137 @@
+// noalloc.cu — a wavefront render entry point that allocates nothing.
+//
+// orn_render_noalloc renders with the persistent wavefront (wavefront.cu)
+// into device buffers the caller provides, for callers that cannot allocate
+// device memory while they render: engines whose frame loop must not call
+// cudaMalloc (an allocation can synchronise the device and stall the frame)
+// and hosts that give a plug-in a fixed memory budget.  Its working memory
+// — one path slot per pixel, the ray queue and the iteration counters —
+// lives in the file-scope array `g_noalloc_scratch` below, sized for
+// kNoAllocMaxPixels pixels; every GPU that loads the library holds that
+// array (about 15 MiB) until the process exits.
+//
+// Host code cannot use the array's name as a device address, so the first
+// call on each device looks the address up with cudaGetSymbolAddress (with
+// that device current) and keeps it; that first call should come before
+// any stream capture.  Every call shares the one array: the call clears the
+// parts that must start at zero, and calls whose work overlaps on the GPU
+// (different streams, or another thread) race on it.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "ornament_cuda.h"
+#include "pt_kernels.h"
+
+namespace {
+
+constexpr uint32_t kNoAllocMaxPixels = ORN_NOALLOC_MAX_PIXELS;
+
+// Byte layout of the scratch array (each region 256-byte aligned).
+constexpr size_t kAlign = 256;
+constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+constexpr size_t kOffCounters = 0;                                            // pixel counter + qstat
+constexpr size_t kOffQueue = align_up(kOffCounters + 20 * sizeof(uint32_t));
+constexpr size_t kOffMode = align_up(kOffQueue + (size_t)kNoAllocMaxPixels * 4);
+constexpr size_t kOffPixel = align_up(kOffMode + (size_t)kNoAllocMaxPixels * 4);
+constexpr size_t kOffKb = align_up(kOffPixel + (size_t)kNoAllocMaxPixels * 4);
+constexpr size_t kOffRngState = align_up(kOffKb + (size_t)kNoAllocMaxPixels * 8);
+constexpr size_t kOffAccum = align_up(kOffRngState + (size_t)kNoAllocMaxPixels * 4);
+constexpr size_t kOffColor = align_up(kOffAccum + (size_t)kNoAllocMaxPixels * 16);
+constexpr size_t kOffRo = align_up(kOffColor + (size_t)kNoAllocMaxPixels * 16);
+constexpr size_t kOffRd = align_up(kOffRo + (size_t)kNoAllocMaxPixels * 16);
+constexpr size_t kOffHit = align_up(kOffRd + (size_t)kNoAllocMaxPixels * 16);
+constexpr size_t kScratchBytes = align_up(kOffHit + (size_t)kNoAllocMaxPixels * 32);
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `device` (looked up once, with the
+// device current).
+cudaError_t scratch_address(int device, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_addr[device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[device] = (unsigned char*)ptr;
+    }
+    *out = g_scratch_addr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+// The scene of a context (capi.cu); declared here to keep the context type
+// private to capi.cu.
+namespace orn {
+const SceneDev* context_scene(const orn_context* ctx, int* device, uint32_t* semantics, uint32_t** error_word,
+                              bool* fast_slabs, const orn_camera* camera);
+}
+
+extern "C" int orn_render_noalloc(const orn_context* ctx, const orn_constant_params* params, uint32_t spp,
+                                  float* accumulation, uint32_t* rng_state, float* framebuffer, void* stream) {
+    if (!ctx || !params || !accumulation || !rng_state || !framebuffer || spp == 0) return ORN_ERR_INVALID_ARGUMENT;
+    const uint64_t pixels = (uint64_t)params->width * params->height;
+    if (pixels == 0 || pixels > kNoAllocMaxPixels) return ORN_ERR_INVALID_ARGUMENT;
+    int device = 0;
+    uint32_t semantics = 0;
+    uint32_t* error_word = nullptr;
+    bool fast = false;
+    const orn::SceneDev* scene = orn::context_scene(ctx, &device, &semantics, &error_word, &fast, &params->camera);
+    if (!scene || device < 0 || device >= kMaxDevices) return ORN_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess) return ORN_ERR_CUDA;
+    unsigned char* base = nullptr;
+    if (scratch_address(device, &base) != cudaSuccess) return ORN_ERR_CUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+
+    orn::WaveLaunch w;
+    std::memset(&w, 0, sizeof(w));
+    w.scene = *scene;
+    w.cp = *params;
+    w.spp = spp;
+    w.do_post = 1;
+    w.pixel_count = (uint32_t)pixels;
+    w.slots = (uint32_t)pixels;
+    w.acc = (float4*)accumulation;
+    w.fb = (float4*)framebuffer;
+    w.rng = rng_state;
+    w.error = error_word;
+    w.counters = nullptr;
+    w.pixel_counter = (uint32_t*)(base + kOffCounters);
+    w.qstat = (uint32_t*)(base + kOffCounters) + 4;
+    w.queue = (uint32_t*)(base + kOffQueue);
+    w.mode = (uint32_t*)(base + kOffMode);
+    w.pixel = (uint32_t*)(base + kOffPixel);
+    w.kb = (uint2*)(base + kOffKb);
+    w.rng_state = (uint32_t*)(base + kOffRngState);
+    w.accum = (float4*)(base + kOffAccum);
+    w.color = (float4*)(base + kOffColor);
+    w.ro = (float4*)(base + kOffRo);
+    w.rd = (float4*)(base + kOffRd);
+    w.hit = (float4*)(base + kOffHit);
+    w.fetch_threshold = orn::kFetchThreshold;
+
+    // What must start at zero: the counters and every slot's mode.
+    if (cudaMemsetAsync(base + kOffCounters, 0, 20 * sizeof(uint32_t), s) != cudaSuccess) return ORN_ERR_CUDA;
+    if (cudaMemsetAsync(w.mode, 0, (size_t)pixels * 4, s) != cudaSuccess) return ORN_ERR_CUDA;
+    // One slot per pixel: every pixel starts in the first iteration and a
+    // pixel casts at most spp * depth rays, one per iteration, so
+    // spp * (depth + 1) + 2 iterations finish the render (iterations after
+    // the last ray find an empty queue and return at once).  No readback.
+    const uint64_t iterations = (uint64_t)spp * ((uint64_t)params->depth + 1) + 2;
+    for (uint64_t it = 0; it < iterations; ++it) {
+        if (orn::launch_wf_logic(w, (uint32_t)it, (int)semantics, orn::MATH_PORTABLE, false, s) != cudaSuccess)
+            return ORN_ERR_CUDA;
+        if (orn::launch_wf_extend(w, (uint32_t)it, false, fast, s) != cudaSuccess) return ORN_ERR_CUDA;
+    }
+    return ORN_OK;
+}
