@@ -277,6 +277,31 @@ int orn_get_stream(const orn_context* ctx, void** stream);
 /* Number of kernel launches the context has issued since creation. */
 int orn_launch_count(const orn_context* ctx, uint64_t* launches);
 
+/* ---- FP64 reference and error -------------------------------------------
+ * The image-quality oracle of SURVEY's configurations: `spp` passes from a
+ * fresh start (RNG seeded with the pixel index, current_iteration 1..spp)
+ * with the context's resolution, State and camera, accumulated in FP64 on
+ * the GPU (the only FP64 in the renderer besides the error reduction);
+ * writes the per-pixel FP64 mean RGBA (4 doubles per pixel) to host memory.
+ * The context's own progressive target is not touched.  Synchronous. */
+int orn_render_f64(orn_context* ctx, uint32_t spp, double* mean_rgba, size_t pixel_count);
+
+/* relMSE of the context's current accumulation (per-pixel mean = sum / count)
+ * against a reference mean (host, 4 doubles per pixel, e.g. from
+ * orn_render_f64): mean over pixels and RGB of (x - r)^2 / (r^2 + 1e-2),
+ * reduced in FP64 on the GPU.  Synchronous. */
+int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel_count, double* relmse);
+
+/* One-tile tensor-core GEMM self-test (no counterpart in the reference):
+ * D[128 x N] = A[128 x K] · B[N x K]^T with 16-bit A, B (F16, or BF16 when
+ * `bf16`), row-major host arrays, FP32 result.  K a multiple of 16 up to
+ * 256, N a multiple of 16 from 16 to 128.  `swap_offsets` exchanges the two
+ * operand-descriptor byte offsets (a deliberately wrong encoding, to show
+ * the test can tell them apart).  Checks the tcgen05 encodings the radiance
+ * cache relies on.  Synchronous; uses device 0. */
+int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int swap_offsets, const uint16_t* A, const uint16_t* B,
+                    float* D);
+
 /* ---- rendering without allocation -----------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory while they render — a frame loop that must never call cudaMalloc

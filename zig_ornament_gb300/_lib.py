@@ -160,6 +160,9 @@ FUNCTIONS = {
     "orn_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "orn_launch_count": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "orn_render_noalloc": (C.c_int, [_P, C.POINTER(ConstantParams), C.c_uint32, _P, _P, _P, _P]),
+    "orn_render_f64": (C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),
+    "orn_tc_selftest": (C.c_int, [C.c_uint32, C.c_uint32, C.c_int, C.c_int, _P, _P, _P]),
+    "orn_relmse": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_double)]),
     "orn_last_error": (C.c_char_p, [_P]),
     "orn_status_string": (C.c_char_p, [C.c_int]),
     "orn_abi_version": (C.c_uint32, []),

@@ -786,6 +786,83 @@ int orn_trace_rays(orn_context* ctx, const orn_ray* rays, size_t count, orn_hit*
     return st;
 }
 
+int orn_render_f64(orn_context* ctx, uint32_t spp, double* mean_rgba, size_t pixel_count) {
+    if (!ctx || !mean_rgba || spp == 0) return ORN_ERR_INVALID_ARGUMENT;
+    if (!ctx->camera_set) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "no camera set (orn_set_camera)");
+    const size_t n = (size_t)ctx->width * ctx->height;
+    if (pixel_count < n) return fail(ctx, ORN_ERR_BUFFER_TOO_SMALL, "mean destination too small");
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    double* acc64 = nullptr;
+    uint32_t* rng = nullptr;
+    int st = [&]() -> int {
+        ORN_CUDA(ctx, cudaMalloc(&acc64, n * 4 * sizeof(double)));
+        ORN_CUDA(ctx, cudaMalloc(&rng, n * sizeof(uint32_t)));
+        ORN_CUDA(ctx, orn::launch_seed_rng(rng, (uint32_t)n, ctx->stream));
+        RenderLaunch p;
+        std::memset(&p, 0, sizeof(p));
+        p.scene = ctx->scene;
+        p.pixel_count = (uint32_t)n;
+        p.rng = rng;
+        p.acc64 = acc64;
+        p.error = ctx->d_error;
+        p.counters = ctx->d_counters;
+        p.work_counter = ctx->d_work;
+        p.shade_threshold = orn::kShadeThreshold;
+        const bool fast = render_fast_slabs(ctx);
+        const uint32_t chunk = 64;
+        for (uint32_t done = 0; done < spp;) {
+            uint32_t k = std::min(chunk, spp - done);
+            p.cp = make_params(ctx, 1.0f + (float)done);
+            p.spp = k;
+            ORN_CUDA(ctx, orn::launch_mega_f64(p, (int)ctx->state.semantics, fast, ctx->stream));
+            ctx->launches++;
+            done += k;
+        }
+        std::vector<double> host(n * 4);
+        ORN_CUDA(ctx, cudaMemcpyAsync(host.data(), acc64, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        int s2 = sync_and_check(ctx);
+        if (s2) return s2;
+        for (size_t i = 0; i < n; ++i) {
+            double w = host[4 * i + 3];
+            for (int c = 0; c < 3; ++c) mean_rgba[4 * i + c] = host[4 * i + c] / w;
+            mean_rgba[4 * i + 3] = 1.0;
+        }
+        return ORN_OK;
+    }();
+    cudaStreamSynchronize(ctx->stream);
+    if (acc64) cudaFree(acc64);
+    if (rng) cudaFree(rng);
+    return st;
+}
+
+int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel_count, double* relmse) {
+    if (!ctx || !reference_mean_rgba || !relmse) return ORN_ERR_INVALID_ARGUMENT;
+    const size_t n = (size_t)ctx->width * ctx->height;
+    if (pixel_count != n) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "reference size does not match the resolution");
+    if (!ctx->target_valid || !ctx->rendered) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "nothing rendered yet");
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    double* ref = nullptr;
+    double* out = nullptr;
+    int st = [&]() -> int {
+        ORN_CUDA(ctx, cudaMalloc(&ref, n * 4 * sizeof(double)));
+        ORN_CUDA(ctx, cudaMalloc(&out, sizeof(double)));
+        ORN_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double), ctx->stream));
+        ORN_CUDA(ctx, cudaMemcpyAsync(ref, reference_mean_rgba, n * 4 * sizeof(double), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        ORN_CUDA(ctx, orn::launch_relmse(ctx->acc, nullptr, ref, (uint32_t)n, out, ctx->stream));
+        double sum = 0.0;
+        ORN_CUDA(ctx, cudaMemcpyAsync(&sum, out, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        int s2 = sync_and_check(ctx);
+        if (s2) return s2;
+        *relmse = sum / (3.0 * (double)n);
+        return ORN_OK;
+    }();
+    cudaStreamSynchronize(ctx->stream);
+    if (ref) cudaFree(ref);
+    if (out) cudaFree(out);
+    return st;
+}
+
 int orn_get_stream(const orn_context* ctx, void** stream) {
     if (!ctx || !stream) return ORN_ERR_INVALID_ARGUMENT;
     *stream = (void*)ctx->stream;

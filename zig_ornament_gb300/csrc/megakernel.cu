@@ -20,12 +20,47 @@ namespace orn {
 
 enum LaneMode { LANE_IDLE = 0, LANE_TRAVERSE = 1, LANE_SHADE = 2, LANE_DONE = 3 };
 
+// Per-pixel accumulation: FP32 RGBA as the reference keeps it
+// (pathtracer.hip.cpp:148-153), or FP64 for the high-sample-count oracle
+// render (orn_render_f64), where only the accumulation is double.
+template <bool F64> struct Accum;
+template <> struct Accum<false> {
+    float4 v;
+    __device__ void load(const RenderLaunch& p, uint32_t gid, float ci0) {
+        v = ci0 > 1.0f ? p.acc[gid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    __device__ void add(float ci, f3 c) {
+        if (ci > 1.0f) v = make_float4(v.x + c.x, v.y + c.y, v.z + c.z, v.w + 1.0f);
+        else v = make_float4(c.x, c.y, c.z, 1.0f);
+    }
+    __device__ void store(const RenderLaunch& p, uint32_t gid) { p.acc[gid] = v; }
+};
+template <> struct Accum<true> {
+    double x, y, z, w;
+    __device__ void load(const RenderLaunch& p, uint32_t gid, float ci0) {
+        if (ci0 > 1.0f) {
+            const double* a = p.acc64 + 4 * (size_t)gid;
+            x = a[0]; y = a[1]; z = a[2]; w = a[3];
+        } else {
+            x = y = z = w = 0.0;
+        }
+    }
+    __device__ void add(float ci, f3 c) {
+        if (ci > 1.0f) { x += (double)c.x; y += (double)c.y; z += (double)c.z; w += 1.0; }
+        else { x = c.x; y = c.y; z = c.z; w = 1.0; }
+    }
+    __device__ void store(const RenderLaunch& p, uint32_t gid) {
+        double* a = p.acc64 + 4 * (size_t)gid;
+        a[0] = x; a[1] = y; a[2] = z; a[3] = w;
+    }
+};
+
 // The render kernel: persistent threads, one path per lane, run as a
 // warp-synchronous state machine (pt_machine.cuh).  Pixels are handed out
 // 32 at a time from p.work_counter; each pixel runs its p.spp passes with the
 // accumulation and RNG state in registers, then writes them back (and the
 // post-processed framebuffer value when p.do_post).
-template <int SEM, int MATH, bool COUNT, bool FAST>
+template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false>
 __global__ void __launch_bounds__(kMegaBlock, kMegaMinBlocks)
 mega_kernel(RenderLaunch p) {
     __shared__ uint32_t sstack[kSmemStack * kMegaBlock];
@@ -42,7 +77,8 @@ mega_kernel(RenderLaunch p) {
     bool exhausted = false;          // warp-uniform: the pixel counter ran out
     uint32_t gid = 0, k = 0, bounce = 0;
     Rng rng{0};
-    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    Accum<F64> acc;
+    acc.load(p, 0, 0.0f);
     f3 ro = mk(0.0f, 0.0f, 0.0f), rd = ro, color = ro;
     HitRec h;
     h.t = 0.0f; h.material = 0; h.type = 0; h.inv = 0; h.tri = 0; h.u = 0.0f; h.v = 0.0f;
@@ -63,17 +99,17 @@ mega_kernel(RenderLaunch p) {
                 walker_begin(w, p.scene, ro, rd);
                 return LANE_TRAVERSE;
             }
-            float ci = ci0 + (float)k;
-            if (ci > 1.0f) acc = make_float4(acc.x + color.x, acc.y + color.y, acc.z + color.z, acc.w + 1.0f);
-            else acc = make_float4(color.x, color.y, color.z, 1.0f);
+            acc.add(ci0 + (float)k, color);
             ++k;
         }
-        p.acc[gid] = acc;
+        acc.store(p, gid);
         p.rng[gid] = rng.state;
-        if (p.do_post) {
-            uint32_t x = gid % W, y = gid / W;
-            uint32_t fbi = p.cp.flip_y != 0 ? W * (H - y - 1) + x : gid;
-            p.fb[fbi] = post_process<SEM, MATH>(acc, ci0 + (float)(p.spp - 1), p.cp.inverted_gamma);
+        if constexpr (!F64) {
+            if (p.do_post) {
+                uint32_t x = gid % W, y = gid / W;
+                uint32_t fbi = p.cp.flip_y != 0 ? W * (H - y - 1) + x : gid;
+                p.fb[fbi] = post_process<SEM, MATH>(acc.v, ci0 + (float)(p.spp - 1), p.cp.inverted_gamma);
+            }
         }
         return LANE_IDLE;
     };
@@ -93,7 +129,7 @@ mega_kernel(RenderLaunch p) {
                 if (mine < p.pixel_count) {
                     gid = mine;
                     rng.state = p.rng[gid];
-                    acc = ci0 > 1.0f ? p.acc[gid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    acc.load(p, gid, ci0);
                     k = 0;
                     mode = start_samples();
                 }
@@ -131,9 +167,7 @@ mega_kernel(RenderLaunch p) {
                     walker_begin(w, p.scene, ro, rd);
                     mode = LANE_TRAVERSE;
                 } else {
-                    float ci = ci0 + (float)k;
-                    if (ci > 1.0f) acc = make_float4(acc.x + color.x, acc.y + color.y, acc.z + color.z, acc.w + 1.0f);
-                    else acc = make_float4(color.x, color.y, color.z, 1.0f);
+                    acc.add(ci0 + (float)k, color);
                     ++k;
                     mode = start_samples();
                 }
@@ -204,17 +238,60 @@ __global__ void post_kernel(const float4* __restrict__ acc, float4* __restrict__
     fb[fbi] = post_process<SEM, MATH>(acc[gid], ci, inv_gamma);
 }
 
+// relMSE against an FP64 reference (SURVEY config metric): per pixel and RGB
+// channel (x - r)^2 / (r^2 + 1e-2) with x the pixel's mean sample value,
+// summed in FP64.
+__global__ void __launch_bounds__(256)
+relmse_kernel(const float4* __restrict__ acc, const double* __restrict__ acc64, const double* __restrict__ ref64,
+              uint32_t n, double* out) {
+    __shared__ double part[256];
+    double sum = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double x[3], w;
+        if (acc64) {
+            const double* a = acc64 + 4 * (size_t)i;
+            w = a[3];
+            x[0] = a[0] / w; x[1] = a[1] / w; x[2] = a[2] / w;
+        } else {
+            float4 a = acc[i];
+            w = (double)a.w;
+            x[0] = (double)a.x / w; x[1] = (double)a.y / w; x[2] = (double)a.z / w;
+        }
+        const double* r = ref64 + 4 * (size_t)i;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            double d = x[c] - r[c];
+            sum += d * d / (r[c] * r[c] + 1e-2);
+        }
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(out, part[0]);
+}
+
+cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* ref64, uint32_t n, double* out,
+                          cudaStream_t s) {
+    uint32_t blocks = (n + 255) / 256;
+    if (blocks > 1216) blocks = 1216;
+    relmse_kernel<<<blocks, 256, 0, s>>>(acc, acc64, ref64, n, out);
+    return cudaGetLastError();
+}
+
 // ---- host-side launchers -----------------------------------------------------
 // Persistent grid: as many blocks as fit on the device at once (never more
 // than the pixels need).
-template <int SEM, int MATH, bool COUNT, bool FAST>
+template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false>
 static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
     static int blocks_per_sm = 0, sms = 0;
     if (blocks_per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST>, kMegaBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST, F64>, kMegaBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     uint32_t need = (p.pixel_count + kMegaBlock - 1) / kMegaBlock;
@@ -222,7 +299,7 @@ static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
     if (need < grid) grid = need;
     cudaError_t e = cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    mega_kernel<SEM, MATH, COUNT, FAST><<<grid, kMegaBlock, 0, s>>>(p);
+    mega_kernel<SEM, MATH, COUNT, FAST, F64><<<grid, kMegaBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -232,6 +309,14 @@ static cudaError_t launch_mega_t(const RenderLaunch& p, bool count, bool fast, c
                            : launch_mega_tt<SEM, MATH_PORTABLE, false, true>(p, s);
     return count ? launch_mega_tt<SEM, MATH_PORTABLE, true, false>(p, s)
                  : launch_mega_tt<SEM, MATH_PORTABLE, false, false>(p, s);
+}
+
+cudaError_t launch_mega_f64(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s) {
+    if (semantics == SEM_WGSL)
+        return fast ? launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, true, true>(p, s)
+                    : launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, false, true>(p, s);
+    return fast ? launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, true, true>(p, s)
+                : launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, false, true>(p, s);
 }
 
 // The render kernels always use the portable transcendentals (bit-exact

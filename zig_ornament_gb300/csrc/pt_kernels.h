@@ -32,6 +32,7 @@ struct RenderLaunch {
     uint32_t* error;
     unsigned long long* counters;
     uint32_t* work_counter;    // next pixel to hand out (zeroed before each launch)
+    double* acc64;             // FP64 accumulation (orn_render_f64 only)
     int shade_threshold;       // ready lanes needed before a warp shades
 };
 
@@ -82,6 +83,12 @@ struct WaveLaunch {
 constexpr int kFetchThreshold = ORN_FETCH_THRESHOLD;
 
 cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, bool fast, cudaStream_t s);
+cudaError_t launch_mega_f64(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s);
+// relMSE = mean over pixels and RGB of (x - r)^2 / (r^2 + 1e-2), with x the
+// per-pixel mean of `acc` (FP32 RGBA sums, or FP64 when acc64) and r of
+// `ref64`; summed in FP64 into *out (zeroed by the caller).
+cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* ref64, uint32_t n,
+                          double* out, cudaStream_t s);
 cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, int math, bool count,
                             cudaStream_t s);
 cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, bool fast, cudaStream_t s);

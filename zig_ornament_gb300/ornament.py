@@ -733,6 +733,21 @@ class Renderer:
         self._check(self._lib.orn_get_counters(self._ctx, out, _lib.COUNTER_COUNT))
         return dict(zip(_lib.COUNTER_NAMES, [int(x) for x in out]))
 
+    def render_f64(self, spp: int) -> np.ndarray:
+        """Per-pixel FP64 mean RGBA of `spp` passes from a fresh start
+        (orn_render_f64)."""
+        n = self.width * self.height
+        out = np.empty((n, 4), dtype=np.float64)
+        self._check(self._lib.orn_render_f64(self._ctx, spp, out.ctypes.data, n))
+        return out
+
+    def relmse(self, reference: np.ndarray) -> float:
+        """relMSE of the current accumulation against an FP64 mean image."""
+        ref = np.ascontiguousarray(reference, dtype=np.float64).reshape(-1, 4)
+        v = C.c_double()
+        self._check(self._lib.orn_relmse(self._ctx, ref.ctypes.data, len(ref), C.byref(v)))
+        return v.value
+
     def stream(self) -> int:
         p = C.c_void_p()
         self._check(self._lib.orn_get_stream(self._ctx, C.byref(p)))
