@@ -160,7 +160,9 @@ enum orn_semantics { ORN_SEMANTICS_HIP = 0, ORN_SEMANTICS_WGSL = 1 };
 /* Kernel variant used by orn_render. */
 enum orn_kernel {
     ORN_KERNEL_MEGA = 0,      /* one thread per pixel, samples looped in-thread */
-    ORN_KERNEL_WAVEFRONT = 1  /* persistent path pool + compacted ray queues   */
+    ORN_KERNEL_WAVEFRONT = 1, /* persistent path pool + compacted ray queues   */
+    ORN_KERNEL_CACHED = 2     /* megakernel + learned radiance cache (orn_attach_cache);
+                                 biased, not bit-exact with the reference     */
 };
 
 /* State, src/state.zig:3-23 (resolution set by orn_set_resolution). */
@@ -289,8 +291,12 @@ int orn_render_f64(orn_context* ctx, uint32_t spp, double* mean_rgba, size_t pix
 /* relMSE of the context's current accumulation (per-pixel mean = sum / count)
  * against a reference mean (host, 4 doubles per pixel, e.g. from
  * orn_render_f64): mean over pixels and RGB of (x - r)^2 / (r^2 + 1e-2),
- * reduced in FP64 on the GPU.  Synchronous. */
-int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel_count, double* relmse);
+ * reduced in FP64 on the GPU.  Pixels whose estimate or reference is not
+ * finite are left out of the mean and counted in *skipped_pixels (may be
+ * NULL): the reference's own sampling occasionally yields a NaN sample,
+ * which stays in that pixel's accumulation.  Synchronous. */
+int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel_count, double* relmse,
+               uint64_t* skipped_pixels);
 
 /* One-tile tensor-core GEMM self-test (no counterpart in the reference):
  * D[128 x N] = A[128 x K] · B[N x K]^T with 16-bit A, B (F16, or BF16 when
@@ -333,6 +339,84 @@ int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int swap_offsets, const ui
 #define ORN_NOALLOC_MAX_PIXELS 131072u
 int orn_render_noalloc(const orn_context* ctx, const orn_constant_params* params, uint32_t spp,
                        float* accumulation, uint32_t* rng_state, float* framebuffer, void* stream);
+
+/* ---- learned radiance cache ----------------------------------------------
+ * No counterpart in the reference (an extension of the renderer).  A small
+ * MLP, trained online on the renderer's own path samples, predicts the
+ * radiance leaving a surface point; with state.kernel = ORN_KERNEL_CACHED,
+ * orn_render ends regular paths at their cache vertex — the first rough
+ * surface hit (lambertian, or metal with fuzz >= 0.25) from the second
+ * vertex on — and adds throughput x surface colour x cache(vertex) instead
+ * of tracing the rest of the path.  Emission, sky and smooth metal/glass
+ * before that vertex are traced as usual, and the cached renderer samples
+ * emissive mesh triangles directly (next-event estimation with multiple
+ * importance sampling, also at the cache vertex), so the network carries
+ * only the light arriving after the cache vertex's scatter.  The estimate
+ * is biased by the cache's error; without the cache (every pixel a training
+ * pixel, train_shift 0) it is unbiased.
+ *
+ * Network: inputs (ORN_CACHE_INPUTS floats, each in [0, 1]) = hit position
+ * normalised to the scene bounds (3), (incoming direction + 1) / 2 (3),
+ * (normal + 1) / 2 (3), roughness (1: lambertian 1, metal fuzz, dielectric
+ * 0); 12-band sin/cos frequency encoding of every input (240 features) plus
+ * the raw inputs, a constant 1 and 5 zeros (256 features); 5 hidden layers
+ * of 64 with ReLU, no biases; 3 outputs (RGB).  Forward in FP16, backward in
+ * BF16, FP32 accumulation (tensor cores), FP32 master weights and Adam.
+ * Loss: relative L2, per channel (y - r)^2 / (y^2 + 0.01) with y held
+ * constant in the denominator; samples whose target r[0] < 0 (or NaN) are
+ * ignored.
+ *
+ * Parameters (ORN_CACHE_PARAM_COUNT FP32 values): the six weight matrices
+ * in order, each row-major [outputs][inputs]: 64 x 256, 4 x (64 x 64), and
+ * the output layer as 16 x 64 whose rows 3..15 are padding (kept zero).
+ *
+ * A cache belongs to one device.  Calls are not thread-safe, and a cache
+ * attached to a context must not be used from another thread while that
+ * context renders.  The host-buffer calls below are synchronous. */
+#define ORN_CACHE_INPUTS 10u
+#define ORN_CACHE_OUTPUTS 3u
+#define ORN_CACHE_PARAM_COUNT 33792u
+
+typedef struct orn_cache orn_cache;
+
+typedef struct orn_cache_config {
+    uint32_t batch;            /* samples per training step, multiple of 128 (default 16384) */
+    uint32_t steps_per_frame;  /* training steps after each cached frame (default 4)          */
+    uint32_t train_shift;      /* one 32-pixel group in 2^train_shift traces full training
+                                  paths each frame (default 4: 1/16 of the pixels)            */
+    float learning_rate;       /* Adam (default 1e-3) */
+    float beta1;               /* default 0.9   */
+    float beta2;               /* default 0.99  */
+    float epsilon;             /* default 1e-8  */
+    uint32_t reserved;         /* 0 */
+} orn_cache_config;
+
+int orn_cache_default_config(orn_cache_config* out);
+/* Creates a cache on `device` (-1: the last device) with weights drawn from
+ * `seed` (He-uniform); `config` may be NULL for the defaults. */
+int orn_cache_create(int device, uint64_t seed, const orn_cache_config* config, orn_cache** out);
+int orn_cache_destroy(orn_cache* cache);
+int orn_cache_set_config(orn_cache* cache, const orn_cache_config* config);
+int orn_cache_get_params(orn_cache* cache, float* dst, size_t count);
+/* Replaces the weights and resets the Adam moments and step count. */
+int orn_cache_set_params(orn_cache* cache, const float* src, size_t count);
+/* outputs[n][3] = network(inputs[n][10]). */
+int orn_cache_infer(orn_cache* cache, const float* inputs, size_t n, float* outputs);
+/* Gradient of the summed loss over the n samples with respect to every
+ * parameter (grads[ORN_CACHE_PARAM_COUNT]) and the summed loss; the weights
+ * are not changed. */
+int orn_cache_gradients(orn_cache* cache, const float* inputs, const float* targets, size_t n, float* grads,
+                        float* loss);
+/* One Adam step on the mean loss over the n samples (n <= 2^20); returns
+ * the summed loss before the step. */
+int orn_cache_train(orn_cache* cache, const float* inputs, const float* targets, size_t n, float* loss);
+/* Adam steps taken and cached frames rendered so far; loss summed over the
+ * last training step (synchronises with the cache's work). */
+int orn_cache_stats(orn_cache* cache, uint64_t* steps, uint64_t* frames, float* last_loss);
+const char* orn_cache_last_error(const orn_cache* cache);
+/* Attaches `cache` (same device; NULL detaches) for ORN_KERNEL_CACHED.
+ * Detach a cache (or destroy the context) before destroying the cache. */
+int orn_attach_cache(orn_context* ctx, orn_cache* cache);
 
 /* ---- errors ------------------------------------------------------------- */
 const char* orn_last_error(const orn_context* ctx);

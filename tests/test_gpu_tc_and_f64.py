@@ -72,10 +72,12 @@ def test_relmse_reduction_and_convergence():
         r.set_state(s)
         r.set_camera(scene.camera.to_struct())
         r.render()
-        e = r.relmse(ref)
+        e, skipped = r.relmse(ref, return_skipped=True)
         acc = r.accumulation().astype(np.float64)
         x = acc[:, :3] / acc[:, 3:4]
-        host = np.mean((x - ref[:, :3]) ** 2 / (ref[:, :3] ** 2 + 1e-2))
+        ok = np.isfinite(x).all(axis=1) & np.isfinite(ref[:, :3]).all(axis=1)
+        assert skipped == int((~ok).sum())
+        host = np.mean((x[ok] - ref[ok, :3]) ** 2 / (ref[ok, :3] ** 2 + 1e-2))
         assert abs(e - host) <= 1e-9 * max(host, 1e-12) + 1e-15
         errs.append(e)
     assert 2.0 < errs[0] / errs[1] < 8.0        # ~1/spp for an unbiased estimator

@@ -28,6 +28,10 @@ SEMANTICS_HIP, SEMANTICS_WGSL = 0, 1
 KERNEL_MEGA, KERNEL_WAVEFRONT = 0, 1
 COUNTER_COUNT = 10
 NOALLOC_MAX_PIXELS = 131072
+CACHE_INPUTS = 10
+CACHE_OUTPUTS = 3
+CACHE_PARAM_COUNT = 33792
+KERNEL_CACHED = 2
 COUNTER_NAMES = ["samples", "rays", "visits", "internal", "sphere_leaf", "mesh_entry", "triangle",
                  "sphere_hits", "mesh_hits", "textured_hits"]
 
@@ -137,6 +141,12 @@ assert C.sizeof(Camera) == 112 and C.sizeof(ConstantParams) == 144
 assert C.sizeof(Ray) == 24 and C.sizeof(Hit) == 32
 
 # name -> (restype, argtypes); every function declared in include/ornament_cuda.h
+class CacheConfig(C.Structure):
+    _fields_ = [("batch", C.c_uint32), ("steps_per_frame", C.c_uint32), ("train_shift", C.c_uint32),
+                ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
+                ("epsilon", C.c_float), ("reserved", C.c_uint32)]
+
+
 _P = C.c_void_p
 FUNCTIONS = {
     "orn_create": (C.c_int, [_P, C.c_int, C.POINTER(C.c_void_p)]),
@@ -162,7 +172,19 @@ FUNCTIONS = {
     "orn_render_noalloc": (C.c_int, [_P, C.POINTER(ConstantParams), C.c_uint32, _P, _P, _P, _P]),
     "orn_render_f64": (C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),
     "orn_tc_selftest": (C.c_int, [C.c_uint32, C.c_uint32, C.c_int, C.c_int, _P, _P, _P]),
-    "orn_relmse": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_double)]),
+    "orn_relmse": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
+    "orn_cache_default_config": (C.c_int, [C.POINTER(CacheConfig)]),
+    "orn_cache_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(CacheConfig), C.POINTER(C.c_void_p)]),
+    "orn_cache_destroy": (C.c_int, [_P]),
+    "orn_cache_set_config": (C.c_int, [_P, C.POINTER(CacheConfig)]),
+    "orn_cache_get_params": (C.c_int, [_P, _P, C.c_size_t]),
+    "orn_cache_set_params": (C.c_int, [_P, _P, C.c_size_t]),
+    "orn_cache_infer": (C.c_int, [_P, _P, C.c_size_t, _P]),
+    "orn_cache_gradients": (C.c_int, [_P, _P, _P, C.c_size_t, _P, C.POINTER(C.c_float)]),
+    "orn_cache_train": (C.c_int, [_P, _P, _P, C.c_size_t, C.POINTER(C.c_float)]),
+    "orn_cache_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_float)]),
+    "orn_cache_last_error": (C.c_char_p, [_P]),
+    "orn_attach_cache": (C.c_int, [_P, _P]),
     "orn_last_error": (C.c_char_p, [_P]),
     "orn_status_string": (C.c_char_p, [C.c_int]),
     "orn_abi_version": (C.c_uint32, []),

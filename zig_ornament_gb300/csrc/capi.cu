@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -22,6 +23,7 @@
 
 #include "ornament_cuda.h"
 #include "pt_kernels.h"
+#include "rc_host.h"
 
 using orn::RenderLaunch;
 using orn::SceneDev;
@@ -37,6 +39,7 @@ struct orn_context {
     uint32_t tlas_len = 0, blas_len = 0;
     double world_extent = 0.0;        // largest |coordinate| of the TLAS bounds
     double max_inverse_entry = 0.0;   // largest |entry| of the inverse transforms
+    float scene_lo[3] = {0.0f, 0.0f, 0.0f}, scene_hi[3] = {0.0f, 0.0f, 0.0f};   // TLAS bounds
 
     orn_state state{};
     orn_camera camera{};
@@ -63,6 +66,22 @@ struct orn_context {
     bool rendered = false;
     uint64_t launches = 0;
     std::string last_error;
+    // radiance cache (ORN_KERNEL_CACHED): the attached cache, the query queue
+    // (one entry per pixel at most) and the training slots
+    orn_cache* cache = nullptr;
+    uint32_t cq_pixels = 0, cq_slots = 0, cq_shift = 0;
+    uint32_t* cq_count = nullptr;
+    uint32_t* cq_pixel = nullptr;
+    float* cq_in = nullptr;
+    float4* cq_thr = nullptr;
+    float* ct_in = nullptr;
+    float* ct_target = nullptr;
+    // emitters the cached renderer samples directly (build_lights)
+    uint32_t light_count = 0;
+    float light_area = 0.0f;
+    const float4* d_lights = nullptr;
+    const float* d_light_cdf = nullptr;
+    const uint32_t* d_light_material = nullptr;
 };
 
 namespace {
@@ -174,6 +193,88 @@ int upload(orn_context* ctx, const T* host, size_t count, T** dev) {
     return ORN_OK;
 }
 
+// Light list of the cached renderer's next-event estimation: every triangle
+// of every mesh leaf of the TLAS whose material is an untextured diffuse
+// light, in world space (object vertices times the leaf's forward transform,
+// the second matrix of its pair), as (v0, e1 = v1 - v0, e2 = v2 - v0) with
+// the emission in the .w components and the leaf's inverse-transform id
+// (what a hit on it records), plus the cumulative areas and a flag per
+// material (1 = its mesh emitters are in the list).
+int build_lights(orn_context* ctx, const orn_scene_blob* b) {
+    std::vector<uint32_t> flag(std::max<uint32_t>(b->materials_len, 1u), 0u);
+    auto nee_material = [&](uint32_t m) {
+        if (m >= b->materials_len) return false;
+        const orn_material& mat = b->materials[m];
+        return mat.type == ORN_DIFFUSE_LIGHT && mat.albedo_texture_index >= b->textures_len;
+    };
+    std::vector<float4> tris;
+    std::vector<float> cdf;
+    double total = 0.0;
+    for (uint32_t i = 0; i < b->tlas_nodes_len; ++i) {
+        const orn_bvh_node& leaf = b->tlas_nodes[i];
+        if (leaf.node_type != ORN_NODE_MESH || !nee_material(leaf.right_or_material_index)) continue;
+        const uint32_t mid = leaf.right_or_material_index;
+        flag[mid] = 1u;
+        const size_t fid = (size_t)leaf.transform_id * 2 + 1;
+        if (fid >= b->transforms_len) continue;
+        const float* F = b->transforms + fid * 16;
+        auto world = [&](const float* v) {
+            double r[3];
+            for (int k = 0; k < 3; ++k)
+                r[k] = (double)F[4 * k] * v[0] + (double)F[4 * k + 1] * v[1] + (double)F[4 * k + 2] * v[2] +
+                       (double)F[4 * k + 3];
+            return std::array<double, 3>{r[0], r[1], r[2]};
+        };
+        const orn_material& mat = b->materials[mid];
+        std::vector<uint32_t> stack{leaf.left_or_custom_id};
+        while (!stack.empty()) {
+            const uint32_t n = stack.back();
+            stack.pop_back();
+            if (n >= b->blas_nodes_len) continue;
+            const orn_bvh_node& bn = b->blas_nodes[n];
+            if (bn.node_type == ORN_NODE_INTERNAL) {
+                stack.push_back(bn.left_or_custom_id);
+                stack.push_back(bn.right_or_material_index);
+                continue;
+            }
+            if (bn.node_type != ORN_NODE_TRIANGLE) continue;
+            auto v0 = world(bn.left_aabb_min_or_v0), v1 = world(bn.left_aabb_max_or_v1),
+                 v2 = world(bn.right_aabb_min_or_v2);
+            double e1[3], e2[3];
+            for (int k = 0; k < 3; ++k) {
+                e1[k] = v1[k] - v0[k];
+                e2[k] = v2[k] - v0[k];
+            }
+            const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                         cz = e1[0] * e2[1] - e1[1] * e2[0];
+            const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+            if (!(area > 0.0) || !std::isfinite(area)) continue;
+            tris.push_back(make_float4((float)v0[0], (float)v0[1], (float)v0[2], mat.albedo[0]));
+            tris.push_back(make_float4((float)e1[0], (float)e1[1], (float)e1[2], mat.albedo[1]));
+            tris.push_back(make_float4((float)e2[0], (float)e2[1], (float)e2[2], mat.albedo[2]));
+            uint32_t inv_id = leaf.transform_id * 2u;
+            float inv_f;
+            std::memcpy(&inv_f, &inv_id, 4);
+            tris.push_back(make_float4(inv_f, 0.0f, 0.0f, 0.0f));
+            total += area;
+            cdf.push_back((float)total);
+        }
+    }
+    ctx->light_count = (uint32_t)cdf.size();
+    ctx->light_area = (float)total;
+    float4* dl = nullptr;
+    float* dc = nullptr;
+    uint32_t* dm = nullptr;
+    int s;
+    if ((s = upload(ctx, tris.data(), tris.size(), &dl))) return s;
+    if ((s = upload(ctx, cdf.data(), cdf.size(), &dc))) return s;
+    if ((s = upload(ctx, flag.data(), flag.size(), &dm))) return s;
+    ctx->d_lights = dl;
+    ctx->d_light_cdf = dc;
+    ctx->d_light_material = dm;
+    return ORN_OK;
+}
+
 // Re-lays the reference's BvhNode arrays into the kernel's node array.
 void relayout_nodes(const orn_scene_blob* b, std::vector<float4>* out) {
     const uint32_t T = b->tlas_nodes_len, B = b->blas_nodes_len;
@@ -234,6 +335,19 @@ int ensure_target(orn_context* ctx) {
     return ORN_OK;
 }
 
+void free_cache_buffers(orn_context* ctx) {
+    void* ptrs[] = {ctx->cq_count, ctx->cq_pixel, ctx->cq_in, ctx->cq_thr, ctx->ct_in, ctx->ct_target};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    ctx->cq_count = nullptr;
+    ctx->cq_pixel = nullptr;
+    ctx->cq_in = nullptr;
+    ctx->cq_thr = nullptr;
+    ctx->ct_in = nullptr;
+    ctx->ct_target = nullptr;
+    ctx->cq_pixels = ctx->cq_slots = 0;
+}
+
 void free_target(orn_context* ctx) {
     if (ctx->acc) cudaFree(ctx->acc);
     if (ctx->fb) cudaFree(ctx->fb);
@@ -254,6 +368,7 @@ int sync_and_check(orn_context* ctx) {
         ORN_CUDA(ctx, cudaMemset(ctx->d_error, 0, 4));
         if (err & orn::ERR_STACK)
             return fail(ctx, ORN_ERR_STACK_OVERFLOW, "a ray needed more than 64 traversal stack entries");
+        if (err & orn::ERR_MMA) return fail(ctx, ORN_ERR_TIMEOUT, "a radiance-cache tensor-core wait timed out");
         return fail(ctx, ORN_ERR_TIMEOUT, "a ray exceeded the per-ray node-visit limit");
     }
     return ORN_OK;
@@ -379,6 +494,88 @@ int render_wavefront_sweep(orn_context* ctx, const orn_constant_params& cp, uint
         ORN_CUDA(ctx, cudaEventRecord(ctx->wf_events[r], ctx->stream));
         ORN_CUDA(ctx, orn::launch_wf_extend(w, iter, ctx->counters_enabled, fast, ctx->stream));
         ctx->launches += 2;
+    }
+    return ORN_OK;
+}
+
+// Query queue and training slots of the cached renderer, sized for the
+// current resolution and the cache's training fraction.
+int ensure_cache_buffers(orn_context* ctx) {
+    const uint32_t n = ctx->width * ctx->height;
+    const uint32_t shift = ctx->cache->config.train_shift;
+    if (ctx->cq_count && ctx->cq_pixels == n && ctx->cq_shift == shift) return ORN_OK;
+    free_cache_buffers(ctx);
+    const uint32_t slots = orn::cache_train_slots(n, shift);
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_count, 4));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_pixel, (size_t)n * 4));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_in, (size_t)n * orn::kCacheInputs * 4));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_thr, (size_t)n * sizeof(float4)));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->ct_in, (size_t)slots * orn::kCacheInputs * 4));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->ct_target, (size_t)slots * 3 * 4));
+    // training inputs must stay finite even in slots no path writes
+    ORN_CUDA(ctx, cudaMemsetAsync(ctx->ct_in, 0, (size_t)slots * orn::kCacheInputs * 4, ctx->stream));
+    ctx->cq_pixels = n;
+    ctx->cq_slots = slots;
+    ctx->cq_shift = shift;
+    return ORN_OK;
+}
+
+// `passes` cached frames, each: one sample per pixel with the cached
+// megakernel, the query pass (inference) adding the cached radiance, then
+// up to steps_per_frame training steps on this frame's training slots; the
+// framebuffer is post-processed after the last frame.
+int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_start) {
+    orn_cache* c = ctx->cache;
+    const bool fast = render_fast_slabs(ctx);
+    const uint32_t n = ctx->width * ctx->height;
+    const uint32_t batch = c->config.batch;
+    const uint32_t nb = (ctx->cq_slots + batch - 1) / batch;
+    const uint32_t steps = std::min(c->config.steps_per_frame, nb);
+    p.do_post = 0;
+    p.spp = 1;
+    for (int k = 0; k < 3; ++k) {
+        p.cache.lo[k] = ctx->scene_lo[k];
+        const float ext = ctx->scene_hi[k] - ctx->scene_lo[k];
+        p.cache.inv_extent[k] = ext > 0.0f ? 1.0f / ext : 0.0f;
+    }
+    p.cache.train_shift = ctx->cq_shift;
+    p.cache.query_count = ctx->cq_count;
+    p.cache.query_pixel = ctx->cq_pixel;
+    p.cache.query_in = ctx->cq_in;
+    p.cache.query_thr = ctx->cq_thr;
+    p.cache.train_in = ctx->ct_in;
+    p.cache.train_target = ctx->ct_target;
+    p.cache.train_slots = ctx->cq_slots;
+    p.cache.light_count = ctx->light_count;
+    p.cache.light_area = ctx->light_area;
+    p.cache.lights = ctx->d_lights;
+    p.cache.light_cdf = ctx->d_light_cdf;
+    p.cache.light_material = ctx->d_light_material;
+    for (uint32_t f = 0; f < passes; ++f) {
+        p.cp = make_params(ctx, ci_start + (float)f);
+        p.cache.frame = (uint32_t)c->frames;
+        ORN_CUDA(ctx, cudaMemsetAsync(ctx->cq_count, 0, 4, ctx->stream));
+        // slots no training path writes this frame read as "no target" (NaN)
+        ORN_CUDA(ctx, cudaMemsetAsync(ctx->ct_target, 0xFF, (size_t)ctx->cq_slots * 12, ctx->stream));
+        ORN_CUDA(ctx, orn::launch_mega_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
+        ctx->launches++;
+        int st = orn::cache_apply_queries(c, ctx->cq_count, n, ctx->cq_in, ctx->cq_pixel, ctx->cq_thr, ctx->acc,
+                                          ctx->d_error, ctx->stream);
+        if (st) return fail(ctx, st, c->last_error);
+        for (uint32_t k = 0; k < steps; ++k) {
+            const uint32_t b = (uint32_t)((c->frames * steps + k) % nb);
+            const uint32_t off = b * batch;
+            const uint32_t m = std::min(batch, ctx->cq_slots - off);
+            st = orn::cache_train_step(c, ctx->ct_in + (size_t)off * orn::kCacheInputs, ctx->ct_target + (size_t)off * 3,
+                                       m, true, ctx->d_error, ctx->stream);
+            if (st) return fail(ctx, st, c->last_error);
+        }
+        c->frames++;
+    }
+    if (p.pixel_count) {
+        ORN_CUDA(ctx, orn::launch_post(ctx->acc, ctx->fb, ctx->width, ctx->height, ctx->state.flip_y ? 1u : 0u,
+                                       ci_start + (float)(passes - 1), ctx->state.inverted_gamma,
+                                       (int)ctx->state.semantics, orn::MATH_PORTABLE, ctx->stream));
     }
     return ORN_OK;
 }
@@ -536,6 +733,30 @@ int orn_create(const orn_scene_blob* blob, int device, orn_context** out) {
                     else ctx->world_extent = std::max(ctx->world_extent, v);
                 }
         }
+        // scene bounds (radiance-cache position inputs): the union of the
+        // TLAS internal nodes' child boxes, else +-world_extent
+        {
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for (uint32_t i = 0; i < blob->tlas_nodes_len; ++i) {
+                const orn_bvh_node& n = blob->tlas_nodes[i];
+                if (n.node_type != ORN_NODE_INTERNAL) continue;
+                const float* mins[2] = {n.left_aabb_min_or_v0, n.right_aabb_min_or_v2};
+                const float* maxs[2] = {n.left_aabb_max_or_v1, n.right_aabb_max_or_v3};
+                for (int k = 0; k < 2; ++k)
+                    for (int j = 0; j < 3; ++j) {
+                        if (std::isfinite(mins[k][j])) lo[j] = std::min(lo[j], (double)mins[k][j]);
+                        if (std::isfinite(maxs[k][j])) hi[j] = std::max(hi[j], (double)maxs[k][j]);
+                    }
+            }
+            for (int j = 0; j < 3; ++j) {
+                if (!(lo[j] <= hi[j])) {
+                    lo[j] = -ctx->world_extent;
+                    hi[j] = ctx->world_extent;
+                }
+                ctx->scene_lo[j] = (float)lo[j];
+                ctx->scene_hi[j] = (float)hi[j];
+            }
+        }
         for (uint32_t t = 0; t < blob->transforms_len; t += 2)
             for (int j = 0; j < 16; ++j) {
                 double v = std::fabs((double)blob->transforms[(size_t)t * 16 + j]);
@@ -557,7 +778,7 @@ int orn_create(const orn_scene_blob* blob, int device, orn_context** out) {
         ctx->scene_textures_count = blob->scene_textures_count;
         ctx->tlas_len = blob->tlas_nodes_len;
         ctx->blas_len = blob->blas_nodes_len;
-        return ORN_OK;
+        return build_lights(ctx, blob);
     }();
     if (st != ORN_OK) {
         orn_destroy(ctx);
@@ -580,6 +801,7 @@ int orn_destroy(orn_context* ctx) {
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_work) cudaFree(ctx->d_work);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
+    free_cache_buffers(ctx);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -589,7 +811,7 @@ int orn_destroy(orn_context* ctx) {
 
 int orn_set_state(orn_context* ctx, const orn_state* s) {
     if (!ctx || !s) return ORN_ERR_INVALID_ARGUMENT;
-    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_WAVEFRONT)
+    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED)
         return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics or kernel");
     ctx->state = *s;
     return ORN_OK;
@@ -637,6 +859,19 @@ int orn_peek_constant_params(const orn_context* ctx, orn_constant_params* out) {
     return ORN_OK;
 }
 
+int orn_attach_cache(orn_context* ctx, orn_cache* cache) {
+    if (!ctx) return ORN_ERR_INVALID_ARGUMENT;
+    if (cache && cache->device != ctx->device)
+        return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "the cache lives on another device");
+    if (ctx->cache != cache) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        free_cache_buffers(ctx);
+    }
+    ctx->cache = cache;
+    return ORN_OK;
+}
+
 int orn_render(orn_context* ctx) {
     if (!ctx) return ORN_ERR_INVALID_ARGUMENT;
     if (!ctx->camera_set) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "no camera set (orn_set_camera)");
@@ -669,6 +904,18 @@ int orn_render(orn_context* ctx) {
     if (ctx->state.kernel == ORN_KERNEL_WAVEFRONT) {
         st = ensure_wavefront(ctx);
         if (st) return st;
+    }
+    if (ctx->state.kernel == ORN_KERNEL_CACHED) {
+        if (!ctx->cache)
+            return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "ORN_KERNEL_CACHED needs a cache (orn_attach_cache)");
+        st = ensure_cache_buffers(ctx);
+        if (st) return st;
+        ORN_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+        st = render_cached(ctx, p, passes, ci_start);
+        if (st) return st;
+        ORN_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+        ctx->rendered = true;
+        return ORN_OK;
     }
     ORN_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
     for (uint32_t done = 0; done < passes;) {
@@ -835,7 +1082,8 @@ int orn_render_f64(orn_context* ctx, uint32_t spp, double* mean_rgba, size_t pix
     return st;
 }
 
-int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel_count, double* relmse) {
+int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel_count, double* relmse,
+               uint64_t* skipped_pixels) {
     if (!ctx || !reference_mean_rgba || !relmse) return ORN_ERR_INVALID_ARGUMENT;
     const size_t n = (size_t)ctx->width * ctx->height;
     if (pixel_count != n) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "reference size does not match the resolution");
@@ -845,16 +1093,18 @@ int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel
     double* out = nullptr;
     int st = [&]() -> int {
         ORN_CUDA(ctx, cudaMalloc(&ref, n * 4 * sizeof(double)));
-        ORN_CUDA(ctx, cudaMalloc(&out, sizeof(double)));
-        ORN_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double), ctx->stream));
+        ORN_CUDA(ctx, cudaMalloc(&out, 2 * sizeof(double)));
+        ORN_CUDA(ctx, cudaMemsetAsync(out, 0, 2 * sizeof(double), ctx->stream));
         ORN_CUDA(ctx, cudaMemcpyAsync(ref, reference_mean_rgba, n * 4 * sizeof(double), cudaMemcpyHostToDevice,
                                       ctx->stream));
         ORN_CUDA(ctx, orn::launch_relmse(ctx->acc, nullptr, ref, (uint32_t)n, out, ctx->stream));
-        double sum = 0.0;
-        ORN_CUDA(ctx, cudaMemcpyAsync(&sum, out, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        double sums[2] = {0.0, 0.0};
+        ORN_CUDA(ctx, cudaMemcpyAsync(sums, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         int s2 = sync_and_check(ctx);
         if (s2) return s2;
-        *relmse = sum / (3.0 * (double)n);
+        const double used = (double)n - sums[1];
+        *relmse = used > 0.0 ? sums[0] / (3.0 * used) : 0.0;
+        if (skipped_pixels) *skipped_pixels = (uint64_t)sums[1];
         return ORN_OK;
     }();
     cudaStreamSynchronize(ctx->stream);

@@ -20,6 +20,21 @@ namespace orn {
 
 enum LaneMode { LANE_IDLE = 0, LANE_TRAVERSE = 1, LANE_SHADE = 2, LANE_DONE = 3 };
 
+// Solid-angle density of the reference's lambertian scatter direction
+// w = normalize(n + s), s = normalize(in_unit_sphere()) (material.hip.h,
+// random.hip.h), whose polar angle about the world z axis is uniform in
+// [0, pi]: p_s(s) = 1 / (2 pi^2 sin(theta_s)).  The map s -> w takes the unit
+// sphere around n (through the origin) to directions with cos(a) = n.w and
+// |n + s| = 2 cos(a), so p(w) = 4 cos(a) p_s(s) with s = 2 cos(a) w - n.
+// (The direction is not cosine-distributed.)
+__device__ __forceinline__ float scatter_pdf(f3 n, f3 w) {
+    const float ca = dot(n, w);
+    if (!(ca > 0.0f)) return 0.0f;
+    const f3 sv = sub(scale(2.0f * ca, w), n);
+    const float sin_s = fmaxf(sqrtf(sv.x * sv.x + sv.y * sv.y), 1e-7f);
+    return 2.0f * ca / (9.8696044f * sin_s);
+}
+
 // Per-pixel accumulation: FP32 RGBA as the reference keeps it
 // (pathtracer.hip.cpp:148-153), or FP64 for the high-sample-count oracle
 // render (orn_render_f64), where only the accumulation is double.
@@ -60,8 +75,14 @@ template <> struct Accum<true> {
 // 32 at a time from p.work_counter; each pixel runs its p.spp passes with the
 // accumulation and RNG state in registers, then writes them back (and the
 // post-processed framebuffer value when p.do_post).
-template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false>
-__global__ void __launch_bounds__(kMegaBlock, kMegaMinBlocks)
+//
+// CACHE: the radiance-cache variant (one sample per pixel; CacheLaunch in
+// pt_kernels.h).  A regular pixel's path stops at its cache vertex (the
+// first rough surface from the second vertex on) and leaves a query there; a
+// training pixel's path runs to the end and records the network inputs at
+// the cache vertex and the radiance that left it.
+template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false>
+__global__ void __launch_bounds__(kMegaBlock, CACHE ? 4 : kMegaMinBlocks)
 mega_kernel(RenderLaunch p) {
     __shared__ uint32_t sstack[kSmemStack * kMegaBlock];
     TravStack<kSmemStack> stack;
@@ -86,6 +107,18 @@ mega_kernel(RenderLaunch p) {
     VisitCount vc = {0, 0, 0, 0, 0};
     SampleCount scn = {0, 0, 0, 0};
     uint32_t err = 0;
+    // radiance cache: the pixel's training slot (or ~0), whether the current
+    // sample recorded its cache vertex, and its throughput up to there
+    uint32_t tslot = 0xffffffffu;
+    bool v2 = false;
+    f3 pre = mk(1.0f, 1.0f, 1.0f);
+    // cached variant: radiance gathered so far (L; Lpre before the cache
+    // vertex), and a pending light sample (its contribution, and the
+    // scattered ray to trace after its shadow ray)
+    f3 L = mk(0.0f, 0.0f, 0.0f), Lpre = L, nee_c = L, sro = L, srd = L, nprev = L;
+    bool shadow = false, nee_prev = false, shadow_end = false, shadow_pre = false;
+    uint32_t shadow_inv = 0;
+    f3 qthr = mk(0.0f, 0.0f, 0.0f);   // a query's throughput x surface colour
 
     // Starts sample k of the current pixel; returns the lane's next mode.
     // Samples with depth 0 finish immediately (the bounce loop never runs).
@@ -94,6 +127,14 @@ mega_kernel(RenderLaunch p) {
             camera_ray<MATH>(p.cp, gid % W, gid / W, rng, &ro, &rd);
             color = mk(1.0f, 1.0f, 1.0f);
             bounce = 0;
+            if (CACHE) {
+                v2 = false;
+                shadow = false;
+                shadow_end = false;
+                shadow_pre = false;
+                nee_prev = false;
+                L = mk(0.0f, 0.0f, 0.0f);
+            }
             if (p.cp.depth > 0) {
                 if (COUNT) scn.rays++;
                 walker_begin(w, p.scene, ro, rd);
@@ -104,7 +145,7 @@ mega_kernel(RenderLaunch p) {
         }
         acc.store(p, gid);
         p.rng[gid] = rng.state;
-        if constexpr (!F64) {
+        if constexpr (!F64 && !CACHE) {
             if (p.do_post) {
                 uint32_t x = gid % W, y = gid / W;
                 uint32_t fbi = p.cp.flip_y != 0 ? W * (H - y - 1) + x : gid;
@@ -131,6 +172,10 @@ mega_kernel(RenderLaunch p) {
                     rng.state = p.rng[gid];
                     acc.load(p, gid, ci0);
                     k = 0;
+                    if constexpr (CACHE) {
+                        tslot = cache_train_slot(gid, p.cache.frame, p.cache.train_shift);
+                        if (tslot >= p.cache.train_slots) tslot = 0xffffffffu;
+                    }
                     mode = start_samples();
                 }
             }
@@ -154,22 +199,242 @@ mega_kernel(RenderLaunch p) {
         const unsigned busy = __ballot_sync(kFull, mode == LANE_TRAVERSE);
         if (ready != 0u && ((int)__popc(ready) >= p.shade_threshold || busy == 0u)) {
             if (mode == LANE_SHADE) {
-                bool cont;
-                if (!w.any) {
-                    if (err) color = mk(0.0f, 0.0f, 0.0f);
-                    else color = sky_color(color, rd);
-                    cont = false;
+                if constexpr (CACHE) {
+                    bool end = false, query = false;
+                    float qin[kCacheInputs];
+                    if (shadow) {
+                        // the shadow ray of a light sample finished: add the sample
+                        // if unoccluded, then trace the scattered ray
+                        shadow = false;
+                        if (w.any && !err && h.type == ORN_NODE_MESH && h.inv == shadow_inv &&
+                            __ldg(p.cache.light_material + h.material) != 0u) {
+                            if (shadow_pre) Lpre = add(Lpre, nee_c);
+                            else L = add(L, nee_c);
+                        }
+                        shadow_pre = false;
+                        if (shadow_end) {
+                            // a regular path's cache vertex: the sample is complete
+                            shadow_end = false;
+                            end = true;
+                        } else {
+                            ro = sro;
+                            rd = srd;
+                            walker_begin(w, p.scene, ro, rd);
+                            mode = LANE_TRAVERSE;
+                        }
+                    } else if (!w.any) {
+                        if (!err) L = add(L, sky_color(color, rd));
+                        end = true;
+                    } else {
+                        const float4 ma = ldg4(p.scene.materials + 2 * (size_t)h.material);
+                        const float4 mb = ldg4(p.scene.materials + 2 * (size_t)h.material + 1);
+                        const uint32_t mtype = bits(mb.z);
+                        const HitGeom g = hit_geometry<MATH, COUNT>(p.scene, h, ro, rd, &scn);
+                        if (mtype > ORN_DIELECTRIC) {
+                            // emitter (or unknown type): the path ends with color x emission,
+                            // unless the previous vertex sampled this emitter directly
+                            f3 c2 = color;
+                            shade_geom<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, g, &ro, &rd, &c2, &scn);
+                            const bool sampled = nee_prev && h.type == ORN_NODE_MESH &&
+                                                 __ldg(p.cache.light_material + h.material) != 0u;
+                            if (sampled) {
+                                // the previous vertex also sampled this emitter: balance-heuristic
+                                // weight of the scattered ray, p_w / (p_w + p_light)
+                                const float rl = sqrtf(dot(rd, rd));
+                                const f3 wd = scale(1.0f / rl, rd);
+                                const float dist = h.t * rl;
+                                const float cl = fabsf(dot(g.normal, wd));
+                                const float pw = scatter_pdf(nprev, wd);
+                                const float pl = cl > 0.0f ? dist * dist / (cl * p.cache.light_area) : 3.0e38f;
+                                c2 = scale(pw / (pw + pl), c2);
+                            }
+                            L = add(L, c2);
+                            end = true;
+                        } else {
+                            const bool rough = mtype == ORN_LAMBERTIAN || (mtype == ORN_METAL && mb.x >= kCacheMinFuzz);
+                            // the surface colour (lambertian and metal attenuation)
+                            auto surface_att = [&]() -> f3 {
+                                const uint32_t tex_id = bits(ma.w);
+                                const bool use_tex = SEM == SEM_WGSL
+                                                         ? (tex_id < p.cp.textures_count && tex_id < p.scene.textures_len)
+                                                         : tex_id < p.scene.textures_len;
+                                return use_tex ? tex_sample(p.scene.textures[tex_id], g.hu, g.hv, SEM == SEM_WGSL)
+                                               : mk(ma.x, ma.y, ma.z);
+                            };
+                            bool at_cache = false;
+                            f3 aclamp = mk(1.0f, 1.0f, 1.0f);
+                            if (bounce >= 1u && !v2 && rough) {
+                                // the cache vertex.  The network learns the radiance that
+                                // leaves it through its scattered ray, divided by the surface
+                                // colour (clamped away from 0), so textures stay exact.
+                                at_cache = true;
+                                const f3 ud = normalize(rd);
+                                const float q[kCacheInputs] = {
+                                    (g.hp.x - p.cache.lo[0]) * p.cache.inv_extent[0],
+                                    (g.hp.y - p.cache.lo[1]) * p.cache.inv_extent[1],
+                                    (g.hp.z - p.cache.lo[2]) * p.cache.inv_extent[2],
+                                    0.5f * (ud.x + 1.0f), 0.5f * (ud.y + 1.0f), 0.5f * (ud.z + 1.0f),
+                                    0.5f * (g.normal.x + 1.0f), 0.5f * (g.normal.y + 1.0f), 0.5f * (g.normal.z + 1.0f),
+                                    mtype == ORN_LAMBERTIAN ? 1.0f : mb.x};
+#pragma unroll
+                                for (int j = 0; j < kCacheInputs; ++j) qin[j] = fminf(fmaxf(q[j], 0.0f), 1.0f);
+                                const f3 a = surface_att();
+                                aclamp = mk(fmaxf(a.x, 1e-3f), fmaxf(a.y, 1e-3f), fmaxf(a.z, 1e-3f));
+                                if (tslot == 0xffffffffu) {
+                                    query = true;
+                                    qthr = mul(color, aclamp);
+                                } else {
+#pragma unroll
+                                    for (int j = 0; j < kCacheInputs; ++j)
+                                        p.cache.train_in[(size_t)tslot * kCacheInputs + j] = qin[j];
+                                }
+                            }
+                            // next-event estimation where the scattered ray is traced
+                            const bool nee = mtype == ORN_LAMBERTIAN && p.cache.light_count > 0u &&
+                                             bounce + 1u < p.cp.depth;
+                            bool shadow_ray = false;
+                            f3 ldir = mk(0.0f, 0.0f, 0.0f);
+                            float ldist = 0.0f;
+                            if (nee) {
+                                const float target = rng.f() * p.cache.light_area;
+                                const float u1 = rng.f(), u2 = rng.f();
+                                uint32_t lo = 0, hi = p.cache.light_count - 1u;
+                                while (lo < hi) {
+                                    const uint32_t mid = (lo + hi) >> 1;
+                                    if (__ldg(p.cache.light_cdf + mid) < target) lo = mid + 1u;
+                                    else hi = mid;
+                                }
+                                const float4 t0 = ldg4(p.cache.lights + 4 * (size_t)lo);
+                                const float4 t1 = ldg4(p.cache.lights + 4 * (size_t)lo + 1);
+                                const float4 t2 = ldg4(p.cache.lights + 4 * (size_t)lo + 2);
+                                shadow_inv = bits(ldg4(p.cache.lights + 4 * (size_t)lo + 3).x);
+                                const f3 e1 = mk(t1.x, t1.y, t1.z), e2 = mk(t2.x, t2.y, t2.z);
+                                const float su = sqrtf(u1);
+                                const f3 y = add(mk(t0.x, t0.y, t0.z), add(scale(su * (1.0f - u2), e1), scale(su * u2, e2)));
+                                const f3 nl = normalize(cross(e1, e2));
+                                const f3 dv = sub(y, g.hp);
+                                const float d2 = dot(dv, dv);
+                                ldist = sqrtf(d2);
+                                ldir = scale(1.0f / ldist, dv);
+                                const float cx = dot(g.normal, ldir), cl = fabsf(dot(nl, ldir));
+                                if (cx > 0.0f && cl > 0.0f && d2 > 0.0f) {
+                                    // balance heuristic: att x Le x p_w / (p_light + p_w),
+                                    // p_light = d^2 / (cos_l A) the light sample's solid-angle
+                                    // density, p_w the scattered ray's
+                                    const float pw = scatter_pdf(g.normal, ldir);
+                                    const float pl = d2 / (cl * p.cache.light_area);
+                                    const float wgt = pw / (pl + pw);
+                                    nee_c = mul(color, mul(surface_att(), scale(wgt, mk(t0.w, t1.w, t2.w))));
+                                    shadow_ray = true;
+                                }
+                            }
+                            const f3 hp = g.hp;
+                            bool trace_shadow = false;
+                            if (query) {
+                                // a regular path ends at its cache vertex: the direct light
+                                // there explicitly, the rest from the cache
+                                if (shadow_ray) {
+                                    trace_shadow = true;
+                                    shadow_end = true;
+                                } else {
+                                    end = true;
+                                }
+                            } else {
+                                if (at_cache) {
+                                    // a training path: from here on gather the radiance the
+                                    // cache learns; this vertex's own light sample counts for
+                                    // the pixel only
+                                    pre = mul(color, aclamp);
+                                    Lpre = L;
+                                    color = mk(1.0f / aclamp.x, 1.0f / aclamp.y, 1.0f / aclamp.z);
+                                    L = mk(0.0f, 0.0f, 0.0f);
+                                    v2 = true;
+                                    shadow_pre = shadow_ray;
+                                }
+                                const bool cont = shade_geom<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, g, &ro, &rd, &color, &scn);
+                                nee_prev = nee;
+                                nprev = g.normal;
+                                if (!cont) {
+                                    end = true;   // absorbed
+                                } else if (++bounce >= p.cp.depth) {
+                                    L = add(L, color);   // depth limit: the reference ends with the throughput
+                                    end = true;
+                                } else if (shadow_ray) {
+                                    trace_shadow = true;
+                                } else {
+                                    walker_begin(w, p.scene, ro, rd);
+                                    mode = LANE_TRAVERSE;
+                                }
+                            }
+                            if (trace_shadow) {
+                                // trace the shadow ray first; (ro, rd) carry it, since the
+                                // walker restores the world ray from them on leaving a BLAS.
+                                // The shadow ray is the very vector the reference's scatter
+                                // would produce toward the light, n + s = 2 cos(a) w, so its
+                                // t_min (in units of that vector) excludes the same
+                                // self-intersections as a scattered ray's.  It searches a
+                                // little past the light point: the sample counts only if the
+                                // closest hit is that emitter, as a scattered ray's emission
+                                // would (coplanar overlapping emitters count once).
+                                const float cx2 = 2.0f * dot(g.normal, ldir);
+                                sro = ro;
+                                srd = rd;
+                                ro = hp;
+                                rd = scale(cx2, ldir);
+                                walker_begin(w, p.scene, ro, rd);
+                                w.t_max = ldist / cx2 * (1.0f + 1e-3f);
+                                shadow = true;
+                                mode = LANE_TRAVERSE;
+                            }
+                        }
+                    }
+                    // append this warp's queries to the queue (one atomic)
+                    const unsigned qm = __ballot_sync(ready, query);
+                    if (qm != 0u) {
+                        const unsigned leader = __ffs(qm) - 1u;
+                        uint32_t base = 0;
+                        if (lane == leader) base = atomicAdd(p.cache.query_count, (unsigned)__popc(qm));
+                        base = __shfl_sync(ready, base, leader);
+                        if (query) {
+                            const uint32_t qi = base + __popc(qm & lanes_below);
+                            p.cache.query_pixel[qi] = gid;
+#pragma unroll
+                            for (int j = 0; j < kCacheInputs; ++j) p.cache.query_in[(size_t)qi * kCacheInputs + j] = qin[j];
+                            p.cache.query_thr[qi] = make_float4(qthr.x, qthr.y, qthr.z, 0.0f);
+                        }
+                    }
+                    if (end) {
+                        // a query's cached radiance is added by the inference pass
+                        f3 c = L;
+                        if (tslot != 0xffffffffu) {
+                            float* tg = p.cache.train_target + (size_t)tslot * 3;
+                            tg[0] = v2 ? L.x : -1.0f;
+                            tg[1] = v2 ? L.y : 0.0f;
+                            tg[2] = v2 ? L.z : 0.0f;
+                            if (v2) c = add(Lpre, mul(pre, L));
+                        }
+                        acc.add(ci0 + (float)k, c);
+                        ++k;
+                        mode = start_samples();
+                    }
                 } else {
-                    cont = shade_hit<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, &ro, &rd, &color, &scn);
-                }
-                if (cont && ++bounce < p.cp.depth) {
-                    if (COUNT) scn.rays++;
-                    walker_begin(w, p.scene, ro, rd);
-                    mode = LANE_TRAVERSE;
-                } else {
-                    acc.add(ci0 + (float)k, color);
-                    ++k;
-                    mode = start_samples();
+                    bool cont;
+                    if (!w.any) {
+                        if (err) color = mk(0.0f, 0.0f, 0.0f);
+                        else color = sky_color(color, rd);
+                        cont = false;
+                    } else {
+                        cont = shade_hit<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, &ro, &rd, &color, &scn);
+                    }
+                    if (cont && ++bounce < p.cp.depth) {
+                        if (COUNT) scn.rays++;
+                        walker_begin(w, p.scene, ro, rd);
+                        mode = LANE_TRAVERSE;
+                    } else {
+                        acc.add(ci0 + (float)k, color);
+                        ++k;
+                        mode = start_samples();
+                    }
                 }
             }
         }
@@ -238,13 +503,17 @@ __global__ void post_kernel(const float4* __restrict__ acc, float4* __restrict__
     fb[fbi] = post_process<SEM, MATH>(acc[gid], ci, inv_gamma);
 }
 
-// relMSE against an FP64 reference (SURVEY config metric): per pixel and RGB
-// channel (x - r)^2 / (r^2 + 1e-2) with x the pixel's mean sample value,
-// summed in FP64.
+// relMSE against an FP64 reference: per pixel and RGB channel
+// (x - r)^2 / (r^2 + 1e-2) with x the pixel's mean sample value, summed in
+// FP64 into out[0]; pixels whose estimate or reference is not finite are
+// skipped and counted in out[1] (as a double).
 __global__ void __launch_bounds__(256)
 relmse_kernel(const float4* __restrict__ acc, const double* __restrict__ acc64, const double* __restrict__ ref64,
               uint32_t n, double* out) {
     __shared__ double part[256];
+    __shared__ unsigned skipped;
+    if (threadIdx.x == 0) skipped = 0;
+    __syncthreads();
     double sum = 0.0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double x[3], w;
@@ -258,6 +527,13 @@ relmse_kernel(const float4* __restrict__ acc, const double* __restrict__ acc64, 
             x[0] = (double)a.x / w; x[1] = (double)a.y / w; x[2] = (double)a.z / w;
         }
         const double* r = ref64 + 4 * (size_t)i;
+        bool finite = true;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) finite = finite && isfinite(x[c]) && isfinite(r[c]);
+        if (!finite) {
+            atomicAdd(&skipped, 1u);
+            continue;
+        }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             double d = x[c] - r[c];
@@ -270,7 +546,10 @@ relmse_kernel(const float4* __restrict__ acc, const double* __restrict__ acc64, 
         if ((int)threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) atomicAdd(out, part[0]);
+    if (threadIdx.x == 0) {
+        atomicAdd(out, part[0]);
+        if (skipped) atomicAdd(out + 1, (double)skipped);
+    }
 }
 
 cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* ref64, uint32_t n, double* out,
@@ -284,14 +563,15 @@ cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* 
 // ---- host-side launchers -----------------------------------------------------
 // Persistent grid: as many blocks as fit on the device at once (never more
 // than the pixels need).
-template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false>
+template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false>
 static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
     static int blocks_per_sm = 0, sms = 0;
     if (blocks_per_sm == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST, F64>, kMegaBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE>,
+                                                      kMegaBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     uint32_t need = (p.pixel_count + kMegaBlock - 1) / kMegaBlock;
@@ -299,8 +579,16 @@ static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
     if (need < grid) grid = need;
     cudaError_t e = cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    mega_kernel<SEM, MATH, COUNT, FAST, F64><<<grid, kMegaBlock, 0, s>>>(p);
+    mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE><<<grid, kMegaBlock, 0, s>>>(p);
     return cudaGetLastError();
+}
+
+cudaError_t launch_mega_cached(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s) {
+    if (semantics == SEM_WGSL)
+        return fast ? launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, true, false, true>(p, s)
+                    : launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, false, false, true>(p, s);
+    return fast ? launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, true, false, true>(p, s)
+                : launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, false, false, true>(p, s);
 }
 
 template <int SEM>

@@ -394,33 +394,32 @@ __device__ __forceinline__ f3 sky_color(f3 color, f3 rd) {
     return mul(color, sky);
 }
 
-// Hit shading and material (pathtracer.hip.cpp:95-145, material.hip.h):
-// returns true when the path continues with the scattered ray in (ro, rd),
-// false when it ends (emission or absorption) with `color` final.
-template <int SEM, int MATH, bool COUNT>
-__device__ __forceinline__ bool shade_hit(const SceneDev& sc, const orn_constant_params& cp, Rng& rng,
-                                          const HitRec& h, f3* ro_io, f3* rd_io, f3* color_io,
-                                          SampleCount* scn) {
-    typedef DevMath<MATH> M;
-    const f3 ro = *ro_io, rd = *rd_io;
-    f3 color = *color_io;
-    uint32_t transform_id = h.inv + 1u;
-    f3 hp = add(ro, scale(h.t, rd));
-    f3 normal;
+// Surface point of a hit (pathtracer.hip.cpp:95-131): position, the normal
+// facing the incoming ray, the side, and the texture coordinates.
+struct HitGeom {
+    f3 hp, normal;
     bool front;
     float hu, hv;
+};
+
+template <int MATH, bool COUNT>
+__device__ __forceinline__ HitGeom hit_geometry(const SceneDev& sc, const HitRec& h, f3 ro, f3 rd, SampleCount* scn) {
+    typedef DevMath<MATH> M;
+    HitGeom g;
+    uint32_t transform_id = h.inv + 1u;
+    g.hp = add(ro, scale(h.t, rd));
     if (h.type == ORN_NODE_SPHERE) {
         if (COUNT) scn->sphere_hits++;
         const float4* m = sc.xforms + 4 * (size_t)transform_id;
         f3 center = mk(dot4(ldg4(m), 0.0f, 0.0f, 0.0f, 1.0f), dot4(ldg4(m + 1), 0.0f, 0.0f, 0.0f, 1.0f),
                        dot4(ldg4(m + 2), 0.0f, 0.0f, 0.0f, 1.0f));
-        f3 on = normalize(sub(hp, center));
+        f3 on = normalize(sub(g.hp, center));
         float theta = M::acos(-on.y);
         float phi = M::atan2(-on.z, on.x) + 3.14159265358979f;
-        hu = phi / (2.0f * 3.14159265358979f);
-        hv = theta / 3.14159265358979f;
-        if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
-        else { normal = on; front = true; }
+        g.hu = phi / (2.0f * 3.14159265358979f);
+        g.hv = theta / 3.14159265358979f;
+        if (dot(rd, on) > 0.0f) { g.normal = neg(on); g.front = false; }
+        else { g.normal = on; g.front = true; }
     } else {
         if (COUNT) scn->mesh_hits++;
         float4 n0 = ldg4(sc.normals + __ldg(sc.normal_indices + h.tri));
@@ -433,17 +432,33 @@ __device__ __forceinline__ bool shade_hit(const SceneDev& sc, const orn_constant
         float nx = w * n0.x + h.u * n1.x + h.v * n2.x;
         float ny = w * n0.y + h.u * n1.y + h.v * n2.y;
         float nz = w * n0.z + h.u * n1.z + h.v * n2.z;
-        hu = w * t0.x + h.u * t1.x + h.v * t2.x;
-        hv = w * t0.y + h.u * t1.y + h.v * t2.y;
+        g.hu = w * t0.x + h.u * t1.x + h.v * t2.x;
+        g.hv = w * t0.y + h.u * t1.y + h.v * t2.y;
         const float4* m = sc.xforms + 4 * (size_t)h.inv;
         float4 m0 = ldg4(m), m1 = ldg4(m + 1), m2 = ldg4(m + 2), m3 = ldg4(m + 3);
         f3 tn = mk(m0.x * nx + m1.x * ny + m2.x * nz + m3.x * 0.0f,
                    m0.y * nx + m1.y * ny + m2.y * nz + m3.y * 0.0f,
                    m0.z * nx + m1.z * ny + m2.z * nz + m3.z * 0.0f);
         f3 on = normalize(tn);
-        if (dot(rd, on) > 0.0f) { normal = neg(on); front = false; }
-        else { normal = on; front = true; }
+        if (dot(rd, on) > 0.0f) { g.normal = neg(on); g.front = false; }
+        else { g.normal = on; g.front = true; }
     }
+    return g;
+}
+
+// Hit shading and material (pathtracer.hip.cpp:95-145, material.hip.h):
+// returns true when the path continues with the scattered ray in (ro, rd),
+// false when it ends (emission or absorption) with `color` final.
+template <int SEM, int MATH, bool COUNT>
+__device__ __forceinline__ bool shade_geom(const SceneDev& sc, const orn_constant_params& cp, Rng& rng,
+                                           const HitRec& h, const HitGeom& g, f3* ro_io, f3* rd_io,
+                                           f3* color_io, SampleCount* scn) {
+    typedef DevMath<MATH> M;
+    const f3 rd = *rd_io;
+    f3 color = *color_io;
+    const f3 hp = g.hp, normal = g.normal;
+    const bool front = g.front;
+    const float hu = g.hu, hv = g.hv;
     float4 ma = ldg4(sc.materials + 2 * (size_t)h.material);
     float4 mb = ldg4(sc.materials + 2 * (size_t)h.material + 1);
     uint32_t mtype = bits(mb.z);
@@ -499,6 +514,14 @@ __device__ __forceinline__ bool shade_hit(const SceneDev& sc, const orn_constant
     }
     *color_io = mul(color, em);
     return false;
+}
+
+template <int SEM, int MATH, bool COUNT>
+__device__ __forceinline__ bool shade_hit(const SceneDev& sc, const orn_constant_params& cp, Rng& rng,
+                                          const HitRec& h, f3* ro_io, f3* rd_io, f3* color_io,
+                                          SampleCount* scn) {
+    const HitGeom g = hit_geometry<MATH, COUNT>(sc, h, *ro_io, *rd_io, scn);
+    return shade_geom<SEM, MATH, COUNT>(sc, cp, rng, h, g, ro_io, rd_io, color_io, scn);
 }
 
 // One whole sample with the straightforward loop structure (used by the

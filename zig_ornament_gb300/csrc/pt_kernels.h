@@ -19,6 +19,66 @@ constexpr int kSmemStack = 32;
 #endif
 constexpr int kMegaMinBlocks = ORN_MEGA_MIN_BLOCKS;   // traversal-stack entries per thread kept in shared memory
 
+// Radiance-cache side of a cached megakernel launch.  Every pixel traces one
+// sample, with next-event estimation: at a lambertian vertex whose scattered
+// ray will be traced, a point on an emissive mesh triangle is sampled by area
+// and connected by a shadow ray; the light sample and a scattered ray from
+// that vertex that hits one of those emitters are combined with the balance
+// heuristic against the density of the reference's own scatter direction
+// (not a cosine lobe: its in_unit_sphere draws the polar angle uniformly,
+// material.hip.h / random.hip.h).  The estimate keeps the reference's
+// expectation, including its depth-limit term.
+//
+// The path's cache vertex is its first rough surface hit (lambertian, or
+// metal with fuzz >= kCacheMinFuzz) from the second vertex on.  The network
+// predicts the radiance leaving that vertex through its scattered ray (the
+// light sample there stays explicit), divided by the surface colour a
+// (clamped to >= 1e-3) so texture detail is not left to the network.  A
+// regular pixel takes its light sample at the cache vertex, appends a query
+// (pixel, network inputs, throughput x a) to the query queue and ends; the
+// inference pass adds throughput x a x cache(inputs) afterwards.  Pixels of
+// the training groups (one warp-sized group of 32 pixels in 2^train_shift,
+// rotating with `frame`) trace the full path instead, record the network
+// inputs at the cache vertex and, at the end of the path, the radiance
+// gathered after the cache vertex's scatter divided by a (the training
+// target) in their training slot.
+constexpr int kCacheInputs = 10;   // position 3, direction 3, normal 3, roughness 1
+constexpr float kCacheMinFuzz = 0.25f;   // metals below this fuzz are not cache vertices
+
+struct CacheLaunch {
+    uint32_t frame;
+    uint32_t train_shift;
+    float lo[3];               // scene bounds: position inputs are (p - lo) * inv_extent
+    float inv_extent[3];
+    uint32_t* query_count;     // zeroed before the launch
+    uint32_t* query_pixel;
+    float* query_in;           // [pixels][10]
+    float4* query_thr;
+    float* train_in;           // [slots][10]
+    float* train_target;       // [slots][3]; x = -1 when the path had no cache vertex
+    uint32_t train_slots;
+    // next-event estimation: emissive mesh triangles, 4 float4 each (v0, e1,
+    // e2 with the emission in .w; the emitter's inverse-transform id in the
+    // x bits of the fourth), their cumulative areas, and a flag per material
+    // whose mesh emitters are in the list
+    uint32_t light_count;
+    float light_area;
+    const float4* lights;
+    const float* light_cdf;
+    const uint32_t* light_material;
+};
+
+// Training slot of pixel `gid` in frame `frame`, or 0xffffffff when the
+// pixel traces a regular (cache-terminated) path.
+__host__ __device__ __forceinline__ uint32_t cache_train_slot(uint32_t gid, uint32_t frame, uint32_t shift) {
+    const uint32_t group = gid >> 5, period = 1u << shift;
+    if (((group + frame) & (period - 1u)) != 0u) return 0xffffffffu;
+    return (group >> shift) * 32u + (gid & 31u);
+}
+__host__ __device__ __forceinline__ uint32_t cache_train_slots(uint32_t pixels, uint32_t shift) {
+    return ((pixels + (32u << shift) - 1u) >> (5 + shift)) * 32u;
+}
+
 // Arguments of one megakernel launch (passed by value).
 struct RenderLaunch {
     SceneDev scene;
@@ -34,6 +94,7 @@ struct RenderLaunch {
     uint32_t* work_counter;    // next pixel to hand out (zeroed before each launch)
     double* acc64;             // FP64 accumulation (orn_render_f64 only)
     int shade_threshold;       // ready lanes needed before a warp shades
+    CacheLaunch cache;         // cached launches only
 };
 
 #ifndef ORN_SHADE_THRESHOLD
@@ -83,10 +144,13 @@ struct WaveLaunch {
 constexpr int kFetchThreshold = ORN_FETCH_THRESHOLD;
 
 cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, bool fast, cudaStream_t s);
+// Cached megakernel launch (one sample per pixel, see CacheLaunch).
+cudaError_t launch_mega_cached(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s);
 cudaError_t launch_mega_f64(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s);
 // relMSE = mean over pixels and RGB of (x - r)^2 / (r^2 + 1e-2), with x the
 // per-pixel mean of `acc` (FP32 RGBA sums, or FP64 when acc64) and r of
-// `ref64`; summed in FP64 into *out (zeroed by the caller).
+// `ref64`; the sum goes to out[0] and the number of skipped (non-finite)
+// pixels to out[1], both FP64 and zeroed by the caller.
 cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* ref64, uint32_t n,
                           double* out, cudaStream_t s);
 cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, int math, bool count,

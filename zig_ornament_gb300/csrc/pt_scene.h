@@ -26,7 +26,7 @@ namespace orn {
 enum { SEM_HIP = 0, SEM_WGSL = 1 };          // enum orn_semantics
 enum { MATH_PORTABLE = 0, MATH_DEVICE = 1 };  // transcendental implementation
 // Error bits written to the context's device error word.
-enum { ERR_STACK = 1u, ERR_VISITS = 2u };
+enum { ERR_STACK = 1u, ERR_VISITS = 2u, ERR_MMA = 4u };   // ERR_MMA: a tensor-core wait timed out
 constexpr uint32_t kRefIndexMask = 0x3FFFFFFFu;
 
 struct TexDesc {

@@ -741,12 +741,14 @@ class Renderer:
         self._check(self._lib.orn_render_f64(self._ctx, spp, out.ctypes.data, n))
         return out
 
-    def relmse(self, reference: np.ndarray) -> float:
-        """relMSE of the current accumulation against an FP64 mean image."""
+    def relmse(self, reference: np.ndarray, return_skipped: bool = False):
+        """relMSE of the current accumulation against an FP64 mean image
+        (non-finite pixels left out; with return_skipped, also their count)."""
         ref = np.ascontiguousarray(reference, dtype=np.float64).reshape(-1, 4)
         v = C.c_double()
-        self._check(self._lib.orn_relmse(self._ctx, ref.ctypes.data, len(ref), C.byref(v)))
-        return v.value
+        k = C.c_uint64()
+        self._check(self._lib.orn_relmse(self._ctx, ref.ctypes.data, len(ref), C.byref(v), C.byref(k)))
+        return (v.value, k.value) if return_skipped else v.value
 
     def stream(self) -> int:
         p = C.c_void_p()
@@ -762,6 +764,97 @@ class Renderer:
         ms = C.c_float()
         self._check(self._lib.orn_last_render_ms(self._ctx, C.byref(ms)))
         return ms.value
+
+    def attach_cache(self, cache: Optional["RadianceCache"]):
+        """Attach a RadianceCache for KERNEL_CACHED renders (None detaches)."""
+        self._check(self._lib.orn_attach_cache(self._ctx, cache.handle if cache is not None else None))
+        self._cache = cache   # keep it alive while attached
+
+
+class RadianceCache:
+    """The learned radiance cache (orn_cache_*): a 10-input, 5 x 64 ReLU,
+    3-output MLP with frequency encoding, trained on the tensor cores.
+    Parameters are FP32, six row-major [outputs][inputs] matrices in order
+    (the output layer padded to 16 rows)."""
+
+    PARAM_COUNT = _lib.CACHE_PARAM_COUNT
+
+    def __init__(self, seed: int = 1, device: int = -1, **config):
+        self._lib = _lib.load()
+        cfg = _lib.CacheConfig()
+        self._lib.orn_cache_default_config(C.byref(cfg))
+        for k, v in config.items():
+            setattr(cfg, k, v)
+        h = C.c_void_p()
+        st = self._lib.orn_cache_create(device, seed, C.byref(cfg), C.byref(h))
+        if st != _lib.ORN_OK:
+            raise _lib.OrnamentError(st, self._lib.orn_status_string(st).decode())
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.orn_cache_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != _lib.ORN_OK:
+            msg = self._lib.orn_cache_last_error(self._h).decode() or self._lib.orn_status_string(st).decode()
+            raise _lib.OrnamentError(st, msg)
+
+    def set_config(self, **config):
+        cfg = _lib.CacheConfig()
+        self._lib.orn_cache_default_config(C.byref(cfg))
+        for k, v in config.items():
+            setattr(cfg, k, v)
+        self._check(self._lib.orn_cache_set_config(self._h, C.byref(cfg)))
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.PARAM_COUNT, dtype=F32)
+        self._check(self._lib.orn_cache_get_params(self._h, out.ctypes.data, out.size))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=F32).ravel()
+        self._check(self._lib.orn_cache_set_params(self._h, p.ctypes.data, p.size))
+
+    def infer(self, inputs: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(inputs, dtype=F32).reshape(-1, _lib.CACHE_INPUTS)
+        out = np.empty((len(x), _lib.CACHE_OUTPUTS), dtype=F32)
+        self._check(self._lib.orn_cache_infer(self._h, x.ctypes.data, len(x), out.ctypes.data))
+        return out
+
+    def gradients(self, inputs: np.ndarray, targets: np.ndarray):
+        """(grads, summed loss) of the summed relative-L2 loss; no update."""
+        x = np.ascontiguousarray(inputs, dtype=F32).reshape(-1, _lib.CACHE_INPUTS)
+        t = np.ascontiguousarray(targets, dtype=F32).reshape(-1, _lib.CACHE_OUTPUTS)
+        g = np.empty(self.PARAM_COUNT, dtype=F32)
+        loss = C.c_float()
+        self._check(self._lib.orn_cache_gradients(self._h, x.ctypes.data, t.ctypes.data, len(x), g.ctypes.data,
+                                                  C.byref(loss)))
+        return g, loss.value
+
+    def train(self, inputs: np.ndarray, targets: np.ndarray) -> float:
+        """One Adam step on the mean loss; returns the summed loss."""
+        x = np.ascontiguousarray(inputs, dtype=F32).reshape(-1, _lib.CACHE_INPUTS)
+        t = np.ascontiguousarray(targets, dtype=F32).reshape(-1, _lib.CACHE_OUTPUTS)
+        loss = C.c_float()
+        self._check(self._lib.orn_cache_train(self._h, x.ctypes.data, t.ctypes.data, len(x), C.byref(loss)))
+        return loss.value
+
+    def stats(self):
+        steps, frames, loss = C.c_uint64(), C.c_uint64(), C.c_float()
+        self._check(self._lib.orn_cache_stats(self._h, C.byref(steps), C.byref(frames), C.byref(loss)))
+        return {"steps": steps.value, "frames": frames.value, "last_loss": loss.value}
 
 
 class PathTracer:

@@ -233,6 +233,30 @@ def instanced_meshes_scene(width=1920, height=1080, seed=1, n_blas=8, n_instance
     return scene
 
 
+def cornell_box_scene(width=640, height=360, light_radiance=8.0, light_size=3.0) -> Scene:
+    """A closed 10 x 10 x 10 room (white floor, ceiling and back/front walls,
+    red left and green right walls) lit by one square ceiling light, with a
+    glass, a brushed-metal and a white sphere; the camera is inside, so every
+    path bounces until it reaches the light or the depth limit.  Used to
+    measure the radiance cache where multi-bounce light dominates."""
+    scene = Scene()
+    white = scene.lambertian((0.73, 0.73, 0.73, 1.0))
+    red = scene.lambertian((0.65, 0.05, 0.05, 1.0))
+    green = scene.lambertian((0.12, 0.45, 0.15, 1.0))
+    light = scene.diffuseLight((light_radiance, light_radiance, light_radiance, 1.0))
+    walls = [((0, 0, 0), (0, 1, 0), white), ((0, 10, 0), (0, -1, 0), white), ((0, 5, -5), (0, 0, 1), white),
+             ((0, 5, 5), (0, 0, -1), white), ((-5, 5, 0), (1, 0, 0), red), ((5, 5, 0), (-1, 0, 0), green)]
+    for c, n, m in walls:
+        scene.attachMesh(scene.createPlaneMesh(f32x4(*c, 1), 10.0, 10.0, f32x4(*n, 0), m))
+    scene.attachMesh(scene.createPlaneMesh(f32x4(0, 9.98, 0, 1), light_size, light_size, f32x4(0, -1, 0, 0), light))
+    scene.attachSphere(scene.createSphere(f32x4(-2.2, 1.5, -1.5, 1), 1.5, scene.dielectric(1.5)))
+    scene.attachSphere(scene.createSphere(f32x4(2.2, 1.5, -0.5, 1), 1.5,
+                                          scene.metal((0.8, 0.7, 0.6, 1.0), 0.3)))
+    scene.attachSphere(scene.createSphere(f32x4(0.0, 1.0, 1.5, 1), 1.0, white))
+    scene.camera = Camera(f32x4(0, 5, 4.9, 1), f32x4(0, 4, -5, 1), f32x4(0, 1, 0, 0), width / height, 75.0, 0.0, 10.0)
+    return scene
+
+
 def small_test_scene(width=96, height=64, seed=7, textured=True, with_spheres=True) -> Scene:
     """A scene that exercises every node type, material and texture path."""
     scene = Scene()
