@@ -60,6 +60,19 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--kernel", default="mega", choices=["mega", "wavefront"])
+    p.add_argument("--mode", default="throughput", choices=["throughput", "relmse", "cached-frames"],
+                   help="throughput: the Msamples/s line (with the time-to-relMSE block unless "
+                        "--no-relmse); relmse: only the time-to-relMSE measurement; cached-frames: "
+                        "render --frames radiance-cache frames (a profiling workload)")
+    p.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE block")
+    p.add_argument("--relmse-width", type=int, default=640)
+    p.add_argument("--relmse-height", type=int, default=360)
+    p.add_argument("--relmse-target", type=float, default=1e-3)
+    p.add_argument("--relmse-ref-spp", type=int, default=16384)
+    p.add_argument("--relmse-budget", type=float, default=8.0, help="GPU seconds per method at most")
+    p.add_argument("--frames", type=int, default=8, help="cached-frames: timed frames")
+    p.add_argument("--scene", default="instanced", choices=["instanced", "closed-room"],
+                   help="cached-frames: the scene")
     return p.parse_args()
 
 
@@ -340,6 +353,11 @@ def run_ours(args):
                              "the limiter is L1/TEX throughput and issue slots (profiles/)"},
         "clocks": clocks.summary(),
     }
+    if not args.no_relmse and args.kernel == "mega":
+        try:
+            line["time_to_relmse"] = relmse_block(args)
+        except Exception as exc:   # the throughput line stands on its own
+            line["time_to_relmse"] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.no_cpu_baseline:
         v, cores, desc = cpu_baseline(bvh, scene, args, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -351,10 +369,144 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---- time to relMSE ------------------------------------------------------------------
+def relmse_scene(name, w, h):
+    from zig_ornament_gb300 import scenes
+    if name == "closed-room":
+        return scenes.cornell_box_scene(w, h)
+    # the radiance-cache configuration: the 1080p instanced-mesh scene with
+    # three emissive quads (rendered at the harness resolution)
+    return scenes.instanced_meshes_scene(w, h, n_lights=3)
+
+
+def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8):
+    """GPU time each renderer needs to bring the relMSE against an FP64
+    `ref_spp`-sample oracle (orn_render_f64) down to `target`: plain
+    megakernel tracing, the cached renderer without the network (every pixel
+    traces its full path with light sampling: unbiased) and the cached
+    renderer (its warm-up training frames counted).  Progressive rendering
+    in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
+    chunks outside the timed renders; the crossing is interpolated
+    log-linearly between the two chunks around it, or extrapolated as
+    relMSE ~ 1/time past the budget."""
+    import math
+    from zig_ornament_gb300 import _lib, ornament
+
+    scene = relmse_scene(name, w, h)
+    bvh = ornament.Bvh(scene, row_major_transforms=True)
+
+    def renderer(kernel):
+        r = ornament.Renderer(bvh, 0)
+        r.set_resolution(w, h)
+        st = ornament.State()
+        st.depth = depth
+        st.kernel = kernel
+        r.set_state(st.to_struct())
+        r.set_camera(scene.camera.to_struct())
+        return r, st
+
+    t0 = time.time()
+    rr, _ = renderer(_lib.KERNEL_MEGA)
+    ref = rr.render_f64(ref_spp)
+    rr.close()
+    ref_s = time.time() - t0
+    out = {"resolution": f"{w}x{h}", "reference_spp": ref_spp, "reference_seconds": round(ref_s, 1)}
+    for method in ("plain", "light_sampling", "cached"):
+        kernel = _lib.KERNEL_MEGA if method == "plain" else _lib.KERNEL_CACHED
+        r, st = renderer(kernel)
+        cache = None
+        t = 0.0
+        if method != "plain":
+            cfg = {"train_shift": 0, "steps_per_frame": 0} if method == "light_sampling" else {"train_shift": 3}
+            cache = ornament.RadianceCache(seed=1, **cfg)
+            r.attach_cache(cache)
+        if method == "cached":
+            st.iterations = 64   # warm-up training frames, then the accumulation restarts
+            r.set_state(st.to_struct())
+            r.render()
+            t += r.last_render_ms() / 1e3
+            r.set_camera(scene.camera.to_struct())
+        curve, n, chunk = [], 0, 16
+        while True:
+            st.iterations = chunk
+            r.set_state(st.to_struct())
+            r.render()
+            t += r.last_render_ms() / 1e3
+            n += chunk
+            e = r.relmse(ref)
+            curve.append((t, n, e))
+            if e <= target or t >= budget_s:
+                break
+            chunk = min(chunk * 2, 1024)
+        reached = curve[-1][2] <= target
+        if reached and len(curve) > 1:
+            (ta, _, ea), (tb, _, eb) = curve[-2], curve[-1]
+            f = (math.log(ea) - math.log(target)) / max(math.log(ea) - math.log(eb), 1e-12)
+            tt = math.exp(math.log(ta) + f * (math.log(tb) - math.log(ta)))
+        elif reached:
+            tt = curve[-1][0]
+        else:
+            tt = curve[-1][0] * curve[-1][2] / target   # relMSE ~ 1/time
+        out[method] = {"seconds": round(tt, 4), "reached": reached,
+                       "samples_per_pixel": n, "final_relmse": curve[-1][2],
+                       "curve": [[round(a, 4), b, float("%.4g" % c)] for a, b, c in curve]}
+        r.close()
+        if cache is not None:
+            cache.close()
+    out["speedup_cached_vs_plain"] = round(out["plain"]["seconds"] / out["cached"]["seconds"], 3)
+    out["speedup_light_sampling_vs_plain"] = round(out["plain"]["seconds"] / out["light_sampling"]["seconds"], 3)
+    return out
+
+
+def relmse_block(args):
+    res = {"target": args.relmse_target, "metric": "GPU seconds to relMSE <= target vs FP64 oracle",
+           "scenes": {}}
+    for name in ("instanced", "closed-room"):
+        res["scenes"][name] = time_to_relmse(name, args.relmse_width, args.relmse_height, args.relmse_target,
+                                             args.relmse_ref_spp, args.relmse_budget)
+    return res
+
+
+def run_cached_frames(args):
+    """A profiling workload: --frames radiance-cache frames (after 4 warm-up
+    frames) of --scene at --width x --height."""
+    from zig_ornament_gb300 import _lib, ornament
+    scene = relmse_scene(args.scene, args.width, args.height)
+    bvh = ornament.Bvh(scene, row_major_transforms=True)
+    r = ornament.Renderer(bvh, 0)
+    r.set_resolution(args.width, args.height)
+    st = ornament.State()
+    st.depth = args.depth
+    st.kernel = _lib.KERNEL_CACHED
+    cache = ornament.RadianceCache(seed=1)
+    r.attach_cache(cache)
+    r.set_state(st.to_struct())
+    r.set_camera(scene.camera.to_struct())
+    st.iterations = 4
+    r.set_state(st.to_struct())
+    r.render()
+    st.iterations = args.frames
+    r.set_state(st.to_struct())
+    r.render()
+    r.synchronize()
+    print(json.dumps({"mode": "cached-frames", "scene": args.scene, "width": args.width, "height": args.height,
+                      "frames": args.frames, "ms_per_frame": r.last_render_ms() / args.frames,
+                      "cache": cache.stats()}), flush=True)
+    r.attach_cache(None)
+    r.close()
+    cache.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "relmse":
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"mode": "relmse", "time_to_relmse": relmse_block(args)}), flush=True)
+    elif args.mode == "cached-frames":
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_cached_frames(args)
     else:
         run_ours(args)
 
