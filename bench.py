@@ -60,10 +60,15 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--kernel", default="mega", choices=["mega", "wavefront"])
-    p.add_argument("--mode", default="throughput", choices=["throughput", "relmse", "cached-frames"],
+    p.add_argument("--mode", default="throughput", choices=["throughput", "relmse", "cached-frames", "batch"],
                    help="throughput: the Msamples/s line (with the time-to-relMSE block unless "
                         "--no-relmse); relmse: only the time-to-relMSE measurement; cached-frames: "
-                        "render --frames radiance-cache frames (a profiling workload)")
+                        "render --frames radiance-cache frames (a profiling workload); batch: the 64-scene "
+                        "batched renderer against one launch per scene")
+    p.add_argument("--batch-scenes", type=int, default=64)
+    p.add_argument("--batch-spp-divisor", type=int, default=16,
+                   help="batch: each frame renders spp/divisor of every scene's 16-256 samples")
+    p.add_argument("--tune-cache", default=None, help="batch: autotuner JSON cache (default: none)")
     p.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE block")
     p.add_argument("--relmse-width", type=int, default=640)
     p.add_argument("--relmse-height", type=int, default=360)
@@ -497,6 +502,78 @@ def run_cached_frames(args):
     cache.close()
 
 
+def run_batch(args):
+    """The batched-rendering configuration: --batch-scenes independent
+    instanced-mesh scenes (total BLAS triangles log-uniform 1k-2M, 1-1024
+    instances, resolutions from {256^2, 640x360, 1280x720, 1920x1080}, 16-256
+    samples per pixel, depth 8), one frame = spp/divisor passes of every
+    scene.  Sequential: each context's own orn_render (one megakernel launch
+    per scene), summed device times; batched: orn_batch_render (one
+    persistent launch replayed from a CUDA graph, launch shape from the
+    autotuner), device time per frame."""
+    from zig_ornament_gb300 import ornament, scenes
+    t0 = time.time()
+    work = scenes.batch_scenes(count=args.batch_scenes, seed=2)
+    ctxs, samples, nodes = [], 0, 0
+    for sc, w, h, spp in work:
+        bvh = ornament.Bvh(sc, row_major_transforms=True)
+        r = ornament.Renderer(bvh, 0)
+        r.set_resolution(w, h)
+        st = ornament.State()
+        st.depth = args.depth
+        st.iterations = max(1, -(-spp // args.batch_spp_divisor))
+        r.set_state(st.to_struct())
+        r.set_camera(sc.camera.to_struct())
+        ctxs.append(r)
+        samples += w * h * st.iterations
+        blob, keep = bvh.blob()
+        nodes += blob.blas_nodes_len
+        del keep
+    setup_s = time.time() - t0
+    # sequential: one render per context, each timed on its own stream
+    for _ in range(args.warmup):
+        for r in ctxs:
+            r.render()
+            r.synchronize()
+    seq_ms = []
+    for _ in range(args.steps):
+        total = 0.0
+        for r in ctxs:
+            r.render()
+            total += r.last_render_ms()
+        seq_ms.append(total)
+    batch = ornament.Batch(ctxs)
+    t1 = time.time()
+    cfg = batch.tune(args.tune_cache)
+    tune_s = time.time() - t1
+    for _ in range(args.warmup):
+        batch.render()
+    batch.synchronize()
+    bat_ms = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            batch.render()
+            bat_ms.append(batch.last_render_ms())
+    seq = samples / (np.mean(seq_ms) / 1e3) / 1e6
+    bat = samples / (np.mean(bat_ms) / 1e3) / 1e6
+    line = {"mode": "batch", "metric": "Msamples/s, batched scenes", "unit": "Msamples/s",
+            "batched": bat, "sequential": seq, "speedup": bat / seq,
+            "ms_per_frame": {"batched": float(np.mean(bat_ms)), "sequential": float(np.mean(seq_ms))},
+            "steps": args.steps, "warmup": args.warmup,
+            "config": {"workload": f"{len(ctxs)} instanced-mesh scenes, total BLAS triangles log-uniform "
+                                   "1k-2M, 1-1024 instances, resolutions 256^2..1920x1080, 16-256 spp, depth "
+                                   f"{args.depth}; one frame = spp/{args.batch_spp_divisor} passes per scene",
+                       "pixels": int(sum(w * h for _, w, h, _ in work)), "samples_per_frame": int(samples),
+                       "blas_nodes": int(nodes), "launch": cfg, "tune_seconds": round(tune_s, 2),
+                       "setup_seconds": round(setup_s, 1)},
+            "gpu_launches_per_frame": {"batched": 1, "sequential": len(ctxs)},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    batch.close()
+    for r in ctxs:
+        r.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -504,6 +581,9 @@ def main():
     elif args.mode == "relmse":
         if int(os.environ.get("RANK", "0")) == 0:
             print(json.dumps({"mode": "relmse", "time_to_relmse": relmse_block(args)}), flush=True)
+    elif args.mode == "batch":
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_batch(args)
     elif args.mode == "cached-frames":
         if int(os.environ.get("RANK", "0")) == 0:
             run_cached_frames(args)

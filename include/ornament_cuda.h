@@ -418,6 +418,44 @@ const char* orn_cache_last_error(const orn_cache* cache);
  * Detach a cache (or destroy the context) before destroying the cache. */
 int orn_attach_cache(orn_context* ctx, orn_cache* cache);
 
+/* ---- batched rendering ------------------------------------------------------
+ * No counterpart in the reference (which renders one scene per PathTracer).
+ * A batch groups up to ORN_BATCH_MAX contexts of one device (any scenes,
+ * resolutions and `iterations`) and renders one orn_render() of every one of
+ * them in a single persistent launch: each context's accumulation, RNG
+ * states, framebuffer and progress end exactly as orn_render would leave
+ * them (bit for bit), and the contexts' own calls (orn_get_framebuffer, …)
+ * are ordered after the batch's work.  The frame is captured as a CUDA graph
+ * on first use and replayed while the contexts' sizes and the launch shape
+ * stay the same.  All contexts must use the same semantics.
+ * orn_last_render_ms of a context does not cover batched frames; use
+ * orn_batch_last_render_ms. */
+#define ORN_BATCH_MAX 64u
+typedef struct orn_batch orn_batch;
+
+typedef struct orn_batch_config {
+    uint32_t block;            /* threads per block: 64, 128 or 192 (default 128) */
+    uint32_t blocks_per_sm;    /* resident blocks per SM the grid is sized for (default 6) */
+    uint32_t shade_threshold;  /* ready lanes a warp waits for before shading (default 8) */
+    uint32_t tuned;            /* out: 1 when chosen by orn_batch_tune */
+} orn_batch_config;
+
+int orn_get_device(const orn_context* ctx, int* device);
+int orn_batch_create(orn_context* const* contexts, uint32_t count, orn_batch** out);
+int orn_batch_destroy(orn_batch* batch);
+int orn_batch_render(orn_batch* batch);
+int orn_batch_synchronize(orn_batch* batch);
+int orn_batch_last_render_ms(orn_batch* batch, float* ms);
+int orn_batch_get_config(const orn_batch* batch, orn_batch_config* out);
+int orn_batch_set_config(orn_batch* batch, const orn_batch_config* config);
+/* Autotuner: times the candidate launch shapes (block size x resident
+ * blocks x shade threshold) on scratch targets — the contexts are not
+ * touched — and keeps the fastest; with `cache_path`, a JSON file keyed by
+ * device and workload (scene count, pixels, samples) is read first and
+ * updated after tuning.  `chosen` may be NULL. */
+int orn_batch_tune(orn_batch* batch, const char* cache_path, orn_batch_config* chosen);
+const char* orn_batch_last_error(const orn_batch* batch);
+
 /* ---- errors ------------------------------------------------------------- */
 const char* orn_last_error(const orn_context* ctx);
 const char* orn_status_string(int status);

@@ -32,6 +32,7 @@ CACHE_INPUTS = 10
 CACHE_OUTPUTS = 3
 CACHE_PARAM_COUNT = 33792
 KERNEL_CACHED = 2
+BATCH_MAX = 64
 COUNTER_NAMES = ["samples", "rays", "visits", "internal", "sphere_leaf", "mesh_entry", "triangle",
                  "sphere_hits", "mesh_hits", "textured_hits"]
 
@@ -147,6 +148,11 @@ class CacheConfig(C.Structure):
                 ("epsilon", C.c_float), ("reserved", C.c_uint32)]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("block", C.c_uint32), ("blocks_per_sm", C.c_uint32), ("shade_threshold", C.c_uint32),
+                ("tuned", C.c_uint32)]
+
+
 _P = C.c_void_p
 FUNCTIONS = {
     "orn_create": (C.c_int, [_P, C.c_int, C.POINTER(C.c_void_p)]),
@@ -185,6 +191,16 @@ FUNCTIONS = {
     "orn_cache_stats": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_float)]),
     "orn_cache_last_error": (C.c_char_p, [_P]),
     "orn_attach_cache": (C.c_int, [_P, _P]),
+    "orn_get_device": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "orn_batch_create": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_void_p)]),
+    "orn_batch_destroy": (C.c_int, [_P]),
+    "orn_batch_render": (C.c_int, [_P]),
+    "orn_batch_synchronize": (C.c_int, [_P]),
+    "orn_batch_last_render_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "orn_batch_get_config": (C.c_int, [_P, C.POINTER(BatchConfig)]),
+    "orn_batch_set_config": (C.c_int, [_P, C.POINTER(BatchConfig)]),
+    "orn_batch_tune": (C.c_int, [_P, C.c_char_p, C.POINTER(BatchConfig)]),
+    "orn_batch_last_error": (C.c_char_p, [_P]),
     "orn_last_error": (C.c_char_p, [_P]),
     "orn_status_string": (C.c_char_p, [C.c_int]),
     "orn_abi_version": (C.c_uint32, []),

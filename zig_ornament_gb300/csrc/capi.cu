@@ -23,6 +23,7 @@
 
 #include "ornament_cuda.h"
 #include "pt_kernels.h"
+#include "batch.h"
 #include "rc_host.h"
 
 using orn::RenderLaunch;
@@ -608,11 +609,60 @@ const SceneDev* context_scene(const orn_context* ctx, int* device, uint32_t* sem
     return &ctx->scene;
 }
 
+int batch_prepare(orn_context* ctx, BatchView* view, bool* fast_slabs, uint32_t* semantics, int* device,
+                  cudaStream_t batch_stream, bool commit) {
+    if (!ctx || !view) return ORN_ERR_INVALID_ARGUMENT;
+    if (!ctx->camera_set) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "no camera set (orn_set_camera)");
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_target(ctx);
+    if (st) return st;
+    const float ci = ctx->camera_dirty ? 0.0f : ctx->current_iteration;
+    const uint32_t passes = std::max<uint32_t>(ctx->state.iterations, 1u);
+    const float ci_start = ci + 1.0f;
+    if (commit) {
+        ctx->camera_dirty = false;
+        ctx->current_iteration = ci + (float)passes;
+    }
+    view->scene = ctx->scene;
+    view->cp = make_params(ctx, ci_start);
+    view->spp = passes;
+    view->pixel_begin = 0;
+    view->acc = ctx->acc;
+    view->fb = ctx->fb;
+    view->rng = ctx->rng;
+    *fast_slabs = render_fast_slabs(ctx);
+    *semantics = ctx->state.semantics;
+    *device = ctx->device;
+    // the batch stream starts after the context's own queued work
+    cudaEvent_t ev = nullptr;
+    ORN_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(batch_stream, ev, 0);
+    cudaEventDestroy(ev);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "ordering the batch after the context");
+    if (commit) {
+        ctx->rendered = true;
+        ctx->launches++;
+    }
+    return ORN_OK;
+}
+
+int batch_finish(orn_context* ctx, cudaEvent_t done) {
+    ORN_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, done, 0));
+    return ORN_OK;
+}
+
 }  // namespace orn
 
 extern "C" {
 
 uint32_t orn_abi_version(void) { return ORN_ABI_VERSION; }
+
+int orn_get_device(const orn_context* ctx, int* device) {
+    if (!ctx || !device) return ORN_ERR_INVALID_ARGUMENT;
+    *device = ctx->device;
+    return ORN_OK;
+}
 
 const char* orn_status_string(int status) {
     switch (status) {

@@ -857,6 +857,67 @@ class RadianceCache:
         return {"steps": steps.value, "frames": frames.value, "last_loss": loss.value}
 
 
+class Batch:
+    """Renders one render() of many Renderers (up to 64, one device, same
+    semantics) in a single persistent launch replayed as a CUDA graph
+    (orn_batch_*).  Each renderer's image and progress end as its own
+    render() would leave them."""
+
+    def __init__(self, renderers):
+        self._lib = _lib.load()
+        self.renderers = list(renderers)
+        arr = (C.c_void_p * len(self.renderers))(*[r.handle.value for r in self.renderers])
+        h = C.c_void_p()
+        st = self._lib.orn_batch_create(arr, len(self.renderers), C.byref(h))
+        if st != _lib.ORN_OK:
+            raise _lib.OrnamentError(st, self._lib.orn_status_string(st).decode())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.orn_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != _lib.ORN_OK:
+            msg = self._lib.orn_batch_last_error(self._h).decode() or self._lib.orn_status_string(st).decode()
+            raise _lib.OrnamentError(st, msg)
+
+    def render(self):
+        self._check(self._lib.orn_batch_render(self._h))
+
+    def synchronize(self):
+        self._check(self._lib.orn_batch_synchronize(self._h))
+
+    def last_render_ms(self) -> float:
+        ms = C.c_float()
+        self._check(self._lib.orn_batch_last_render_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def config(self) -> dict:
+        c = _lib.BatchConfig()
+        self._check(self._lib.orn_batch_get_config(self._h, C.byref(c)))
+        return {"block": c.block, "blocks_per_sm": c.blocks_per_sm, "shade_threshold": c.shade_threshold,
+                "tuned": bool(c.tuned)}
+
+    def set_config(self, block=128, blocks_per_sm=6, shade_threshold=8):
+        c = _lib.BatchConfig(block, blocks_per_sm, shade_threshold, 0)
+        self._check(self._lib.orn_batch_set_config(self._h, C.byref(c)))
+
+    def tune(self, cache_path: Optional[str] = None) -> dict:
+        c = _lib.BatchConfig()
+        path = str(cache_path).encode() if cache_path else None
+        self._check(self._lib.orn_batch_tune(self._h, path, C.byref(c)))
+        return {"block": c.block, "blocks_per_sm": c.blocks_per_sm, "shade_threshold": c.shade_threshold,
+                "tuned": bool(c.tuned)}
+
+
 class PathTracer:
     """The CUDA backend behind the PathTracer surface
     (src/hip_backend/path_tracer.zig:12-236).

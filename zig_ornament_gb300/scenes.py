@@ -233,6 +233,35 @@ def instanced_meshes_scene(width=1920, height=1080, seed=1, n_blas=8, n_instance
     return scene
 
 
+BATCH_RESOLUTIONS = ((256, 256), (640, 360), (1280, 720), (1920, 1080))
+
+
+def batch_scenes(count=64, seed=2, tri_range=(1_000, 2_000_000), instance_range=(1, 1024), spp_range=(16, 256),
+                 resolutions=BATCH_RESOLUTIONS, texture_size=256):
+    """The batched-rendering workload: `count` independent instanced-mesh
+    scenes (as instanced_meshes_scene), each with its total BLAS triangle
+    count log-uniform in `tri_range` (spread over up to 8 BLAS), an instance
+    count log-uniform in `instance_range`, a resolution drawn from
+    `resolutions` and a sample count log-uniform in `spp_range`.  Returns a
+    list of (scene, width, height, spp).  Textures are `texture_size`^2
+    (procedural, as in the 1080p scene)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        tris = math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))
+        n_blas = int(min(8, max(1, tris // 2_000)))
+        per = tris / n_blas
+        inst = int(round(math.exp(rng.uniform(math.log(instance_range[0]), math.log(instance_range[1])))))
+        w, h = resolutions[int(rng.integers(len(resolutions)))]
+        spp = int(round(math.exp(rng.uniform(math.log(spp_range[0]), math.log(spp_range[1])))))
+        scene = instanced_meshes_scene(w, h, seed=int(rng.integers(1 << 30)), n_blas=n_blas,
+                                       n_instances=max(inst - n_blas, 0),
+                                       tri_range=(max(per * 0.8, 80.0), per * 1.25), n_textures=2,
+                                       texture_size=texture_size)
+        out.append((scene, w, h, spp))
+    return out
+
+
 def cornell_box_scene(width=640, height=360, light_radiance=8.0, light_size=3.0) -> Scene:
     """A closed 10 x 10 x 10 room (white floor, ceiling and back/front walls,
     red left and green right walls) lit by one square ceiling light, with a
