@@ -16,6 +16,9 @@ generated from a numpy PCG64 stream with a fixed seed.
                          quad of radiance 15.
   small_test_scene       a few spheres, meshes, instances and small textures
                          (parity tests).
+  large_scene            4096 instances over 32 BLAS (~10M triangles), 8 quads.
+  batch_scenes           64 scenes of uneven size for the batched renderer.
+  cornell_box_scene      a closed room lit by one ceiling light (radiance cache).
 """
 from __future__ import annotations
 
@@ -140,16 +143,17 @@ def value_noise_texture(size: int, rng: np.random.Generator, octaves: int = 4) -
 
 
 def random_material(scene: Scene, rng: np.random.Generator, textures=(), textured_fraction=0.0,
-                    mix=(0.8, 0.95)):
+                    mix=(0.8, 0.95), fuzz_max=0.5):
     """Sphere-field material mix: lambertian (albedo U^2 per channel), metal
-    (albedo U(0.5, 1), fuzz U(0, 0.5)), dielectric (ior 1.5)."""
+    (albedo U(0.5, 1), fuzz U(0, fuzz_max)), dielectric (ior 1.5); `mix`
+    holds the cumulative lambertian and metal fractions."""
     choose = rng.random()
     if choose < mix[0]:
         if textures and rng.random() < textured_fraction:
             return scene.lambertian(textures[int(rng.integers(len(textures)))])
         return scene.lambertian(tuple((rng.random(3) * rng.random(3)).tolist()) + (1.0,))
     if choose < mix[1]:
-        return scene.metal(tuple((0.5 + 0.5 * rng.random(3)).tolist()) + (1.0,), float(0.5 * rng.random()))
+        return scene.metal(tuple((0.5 + 0.5 * rng.random(3)).tolist()) + (1.0,), float(fuzz_max * rng.random()))
     return scene.dielectric(1.5)
 
 
@@ -196,7 +200,7 @@ def _blas_mesh(rng, target_tris, radius):
 def instanced_meshes_scene(width=1920, height=1080, seed=1, n_blas=8, n_instances=256,
                            tri_range=(10_000, 80_000), n_textures=4, texture_size=1024,
                            box=100.0, n_lights=1, textured_fraction=0.25, mix=(0.8, 0.95),
-                           blas_radius=4.0) -> Scene:
+                           blas_radius=4.0, fuzz_max=0.5, light_size=40.0) -> Scene:
     scene = Scene()
     rng = np.random.default_rng(seed)
     textures = []
@@ -215,22 +219,38 @@ def instanced_meshes_scene(width=1920, height=1080, seed=1, n_blas=8, n_instance
     for _ in range(n_blas):
         target = math.exp(rng.uniform(lo, hi))
         v, n, uv, idx = _blas_mesh(rng, target, blas_radius)
-        mat = random_material(scene, rng, textures, textured_fraction, mix)
+        mat = random_material(scene, rng, textures, textured_fraction, mix, fuzz_max)
         m = scene.createMesh(v, idx, n, idx, uv, idx, random_transform(), mat)
         scene.attachMesh(m)
         meshes.append(m)
     for _ in range(n_instances):
         base = meshes[int(rng.integers(len(meshes)))]
-        mat = random_material(scene, rng, textures, textured_fraction, mix)
+        mat = random_material(scene, rng, textures, textured_fraction, mix, fuzz_max)
         scene.attachMeshInstance(scene.createMeshInstance(base, random_transform(), mat))
     light = scene.diffuseLight((15.0, 15.0, 15.0, 1.0))
     for k in range(n_lights):
         cx = 0.0 if n_lights == 1 else float(rng.uniform(-half * 0.6, half * 0.6))
         cz = 0.0 if n_lights == 1 else float(rng.uniform(-half * 0.6, half * 0.6))
-        scene.attachMesh(scene.createPlaneMesh(f32x4(cx, half + 20.0, cz, 1), 40.0, 40.0, f32x4(0, -1, 0, 0), light))
+        scene.attachMesh(scene.createPlaneMesh(f32x4(cx, half + 20.0, cz, 1), light_size, light_size,
+                                               f32x4(0, -1, 0, 0), light))
     scene.camera = Camera(f32x4(0, 0.45 * box, 1.9 * box, 1), f32x4(0, 0, 0, 1), f32x4(0, 1, 0, 0),
                           width / height, 40.0, 0.0, 1.9 * box)
     return scene
+
+
+def large_scene(width=3840, height=2160, seed=4, n_blas=32, n_instances=4096, total_tris=10_000_000,
+                texture_size=1024) -> Scene:
+    """The large configuration: `n_instances` instances over `n_blas`
+    icosphere/torus BLAS totalling about `total_tris` triangles (each BLAS
+    log-uniform within x0.7..x1.4 of the mean share), materials 40 %
+    dielectric / 30 % metal (fuzz U(0, 0.3)) / 30 % textured lambertian,
+    8 emissive quads.  The box grows to 250 so the instance density matches
+    the 1080p scene's 256 instances in 100^3, and the quads grow with it."""
+    per = total_tris / n_blas
+    return instanced_meshes_scene(width, height, seed=seed, n_blas=n_blas, n_instances=n_instances - n_blas,
+                                  tri_range=(0.7 * per, 1.4 * per), n_textures=4, texture_size=texture_size,
+                                  box=250.0, n_lights=8, textured_fraction=1.0, mix=(0.3, 0.6), fuzz_max=0.3,
+                                  light_size=100.0)
 
 
 BATCH_RESOLUTIONS = ((256, 256), (640, 360), (1280, 720), (1920, 1080))
