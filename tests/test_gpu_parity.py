@@ -324,3 +324,25 @@ def test_full_size_properties_1080p(kernel):
     assert c["sphere_hits"] + c["mesh_hits"] <= c["rays"]
     a.close()
     b.close()
+
+
+def test_large_scene_sampled_pixels_vs_oracle(oracle):
+    """Config-4 scale (4096 instances over ~10M triangles, 3840x2160, depth
+    16): one pass of the megakernel over the whole frame, every 2003rd pixel
+    checked bit for bit against the oracle (accumulation and RNG state)."""
+    w, h, stride = 3840, 2160, 2003
+    scene = scenes.large_scene(w, h)
+    bvh = ornament.Bvh(scene)
+    r = ornament.Renderer(bvh, device=0)
+    r.set_resolution(w, h)
+    r.set_state(make_state(depth=16, iterations=1))
+    r.set_camera(scene.camera.to_struct())
+    r.render()
+    acc, rng, _ = r.progress()
+    cp = ol.make_params(scene.camera, w, h, depth=16, textures_count=bvh.scene_textures_count)
+    oacc, orng, _, _ = oracle.render(bvh, cp, 1, pixel_range=(0, w * h), pixel_stride=stride)
+    idx = np.arange(0, w * h, stride)
+    assert len(idx) > 4000
+    assert np.array_equal(rng[idx], orng[idx])
+    assert np.array_equal(bits(acc[idx]), bits(oacc[idx]))
+    r.close()
