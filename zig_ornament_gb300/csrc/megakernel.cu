@@ -570,6 +570,11 @@ static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#ifdef ORN_MEGA_CARVEOUT
+        // shared-memory share of the unified L1/shared space, in percent
+        cudaFuncSetAttribute(mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout, ORN_MEGA_CARVEOUT);
+#endif
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE>,
                                                       kMegaBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;

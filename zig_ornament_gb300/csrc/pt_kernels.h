@@ -12,12 +12,17 @@
 namespace orn {
 
 constexpr int kMegaBlock = 128;
-constexpr int kSmemStack = 32;
+// Traversal-stack entries per thread kept in shared memory (the rest of the
+// 64-entry stack spills to local memory).
+#ifndef ORN_SMEM_STACK
+#define ORN_SMEM_STACK 32
+#endif
+constexpr int kSmemStack = ORN_SMEM_STACK;
 // Resident blocks per SM the megakernel is compiled for (register cap).
 #ifndef ORN_MEGA_MIN_BLOCKS
 #define ORN_MEGA_MIN_BLOCKS 6
 #endif
-constexpr int kMegaMinBlocks = ORN_MEGA_MIN_BLOCKS;   // traversal-stack entries per thread kept in shared memory
+constexpr int kMegaMinBlocks = ORN_MEGA_MIN_BLOCKS;
 
 // Radiance-cache side of a cached megakernel launch.  Every pixel traces one
 // sample, with next-event estimation: at a lambertian vertex whose scattered
@@ -107,6 +112,7 @@ constexpr int kShadeThreshold = ORN_SHADE_THRESHOLD;
 #define ORN_STEPS_PER_ITERATION 8
 #endif
 constexpr int kStepsPerIteration = ORN_STEPS_PER_ITERATION;
+
 
 // Arguments of one wavefront iteration (wavefront.cu).  Path slots are
 // structure-of-arrays; qstat holds per-iteration [queue count, slots waiting
