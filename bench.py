@@ -57,6 +57,9 @@ def parse():
                    help="instanced: the 1080p instanced-mesh scene (default, the headline); spheres: the "
                         "640x360 sphere field (64 spp, depth 10); large: 4096 instances over ~10M "
                         "triangles at 3840x2160 (depth 16)")
+    p.add_argument("--bvh", default="reference", choices=["reference", "sah"],
+                   help="reference: bvh.zig's tree (the parity tree, default); sah: the binned-SAH tree "
+                        "(non-parity mode: fewer node visits, images equal in expectation)")
     p.add_argument("--spp", type=int, default=None, help="sample passes per step (render iterations)")
     p.add_argument("--width", type=int, default=None)
     p.add_argument("--height", type=int, default=None)
@@ -99,9 +102,9 @@ def apply_workload_defaults(args):
 
 
 def metric_name(args):
-    if args.workload == "instanced" and (args.width, args.height) == (1920, 1080):
+    if args.workload == "instanced" and (args.width, args.height) == (1920, 1080) and args.bvh == "reference":
         return METRIC
-    return f"Msamples/s, {args.workload} {args.width}x{args.height}"
+    return f"Msamples/s, {args.workload} {args.width}x{args.height}" + (", SAH tree" if args.bvh == "sah" else "")
 
 
 def workload(args):
@@ -119,9 +122,10 @@ def workload(args):
         scene = scenes.instanced_meshes_scene(args.width, args.height)
         desc = ("instanced meshes TLAS/BLAS: 8 BLAS icospheres+tori 10k-80k tris, 256 instances, "
                 "4 procedural 1024^2 RGBA8 textures, 1 emissive quad (radiance 15)")
-    bvh = ornament.Bvh(scene)
+    bvh = ornament.Bvh(scene, builder=args.bvh)
     tris = sum(len(m.vertex_indices) // 3 for m in scene.meshes)
-    cfg = {"workload": desc,
+    cfg = {"workload": desc, "bvh": ("bvh.zig rules (random axis, median split): the parity tree"
+                                     if args.bvh == "reference" else "binned SAH (non-parity mode)"),
            "resolution": f"{args.width}x{args.height}", "spp_per_step": args.spp, "depth": args.depth,
            "triangles": tris, "instances": len(scene.mesh_instances), "blas": len(scene.meshes),
            "tlas_nodes": int(len(bvh.tlas_nodes)), "blas_nodes": int(len(bvh.blas_nodes)),
@@ -395,10 +399,11 @@ def run_ours(args):
                               "the limiter is L1/TEX throughput and issue slots (profiles/)")
                              if args.workload != "large" else
                              ("1.3 GB of BVH nodes do not fit the 129 MB L2: node fetches go to HBM; "
-                              "latency-bound at 317 node visits per ray (profiles/)")},
+                              f"latency-bound at {counters['visits'] / max(counters['rays'], 1):.0f} node "
+                              "visits per ray (profiles/)")},
         "clocks": clocks.summary(),
     }
-    if not args.no_relmse and args.kernel == "mega" and args.workload == "instanced":
+    if not args.no_relmse and args.kernel == "mega" and args.workload == "instanced" and args.bvh == "reference":
         try:
             line["time_to_relmse"] = relmse_block(args)
         except Exception as exc:   # the throughput line stands on its own

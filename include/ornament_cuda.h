@@ -513,7 +513,18 @@ typedef struct orn_scene_desc {
     const orn_texture* textures;                  uint32_t textures_len;
     uint64_t seed;                /* split-axis PRNG seed (bvh.zig uses 1244) */
     uint32_t row_major_transforms;/* 1 = HIP layout (transposed), 0 = wgpu   */
+    uint32_t builder;             /* enum orn_bvh_builder, default REFERENCE */
 } orn_scene_desc;
+
+/* Tree builder.  REFERENCE follows bvh.zig's rules (random split axis,
+ * median of aabb.min): the tree every parity claim is made on.  SAH is a
+ * non-parity mode with no counterpart in the reference: binned
+ * surface-area-heuristic splits over the same node format (one primitive
+ * per leaf, 2n-1 nodes, children before parents), so the kernels run it
+ * unchanged with fewer node visits; images agree with the reference's in
+ * expectation, not bit for bit (equal-distance hits may resolve to another
+ * primitive and visit counts differ). */
+enum orn_bvh_builder { ORN_BVH_REFERENCE = 0, ORN_BVH_SAH = 1 };
 
 typedef struct orn_bvh orn_bvh;
 

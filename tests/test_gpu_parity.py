@@ -346,3 +346,23 @@ def test_large_scene_sampled_pixels_vs_oracle(oracle):
     assert np.array_equal(rng[idx], orng[idx])
     assert np.array_equal(bits(acc[idx]), bits(oacc[idx]))
     r.close()
+
+
+@pytest.mark.parametrize("kernel", KERNELS, ids=KERNEL_IDS)
+def test_sah_tree_renders_like_the_oracle(oracle, kernel):
+    """The non-parity SAH tree runs through the same kernels: bit for bit
+    what the oracle's traversal gives on that tree."""
+    scene = scenes.instanced_meshes_scene(96, 54, seed=1, n_blas=4, n_instances=40, tri_range=(2000, 8000),
+                                          texture_size=128)
+    bvh = ornament.Bvh(scene, builder="sah")
+    r = ornament.Renderer(bvh, device=0)
+    r.set_resolution(96, 54)
+    r.set_state(make_state(depth=8, gamma=2.2, iterations=2, kernel=kernel))
+    r.set_camera(scene.camera.to_struct())
+    r.render()
+    acc, rng, _ = r.progress()
+    cp = ol.make_params(scene.camera, 96, 54, depth=8, gamma=2.2, textures_count=bvh.scene_textures_count)
+    oacc, orng, _, _ = oracle.render(bvh, cp, 2)
+    assert np.array_equal(rng, orng)
+    assert np.array_equal(bits(acc), bits(oacc))
+    r.close()

@@ -33,6 +33,7 @@ CACHE_OUTPUTS = 3
 CACHE_PARAM_COUNT = 33792
 KERNEL_CACHED = 2
 BATCH_MAX = 64
+BVH_REFERENCE, BVH_SAH = 0, 1
 COUNTER_NAMES = ["samples", "rays", "visits", "internal", "sphere_leaf", "mesh_entry", "triangle",
                  "sphere_hits", "mesh_hits", "textured_hits"]
 
@@ -133,7 +134,7 @@ class SceneDesc(C.Structure):
                 ("mesh_instances", C.c_void_p), ("mesh_instances_len", C.c_uint32),
                 ("materials", C.c_void_p), ("materials_len", C.c_uint32),
                 ("textures", C.c_void_p), ("textures_len", C.c_uint32),
-                ("seed", C.c_uint64), ("row_major_transforms", C.c_uint32)]
+                ("seed", C.c_uint64), ("row_major_transforms", C.c_uint32), ("builder", C.c_uint32)]
 
 
 # src/gpu_structs.zig layouts: BvhNode 64 B, Material 32 B, Camera 112 B, ConstantParams 144 B

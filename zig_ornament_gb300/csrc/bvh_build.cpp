@@ -135,6 +135,89 @@ bool finite3(const float* v) {
     return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
 }
 
+// ---- binned SAH split (the non-parity builder) -------------------------------
+// Partitions items[0..n) in place into a left and a right part and returns
+// the left count (1..n-1): centroids are binned (up to 32 bins) along each
+// axis with a non-zero centroid extent, and the bin boundary minimising
+// area(left) * count(left) + area(right) * count(right) is taken; items whose
+// centroids coincide are split in half.  `box(item, mn, mx)` gives an item's
+// bounds.
+template <class T, class Box>
+size_t sah_split(T* items, size_t n, Box box) {
+    float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t i = 0; i < n; ++i) {
+        float mn[3], mx[3];
+        box(items[i], mn, mx);
+        for (int k = 0; k < 3; ++k) {
+            const float c = 0.5f * (mn[k] + mx[k]);
+            cmin[k] = std::min(cmin[k], c);
+            cmax[k] = std::max(cmax[k], c);
+        }
+    }
+    constexpr int kBins = 32;
+    const int bins = (int)std::min<size_t>(kBins, std::max<size_t>(n, 2));
+    double best_cost = INFINITY;
+    int best_axis = -1, best_bin = 0;
+    auto area = [](const float* mn, const float* mx) {
+        const double dx = (double)mx[0] - mn[0], dy = (double)mx[1] - mn[1], dz = (double)mx[2] - mn[2];
+        return dx < 0 ? 0.0 : 2.0 * (dx * dy + dy * dz + dz * dx);
+    };
+    for (int axis = 0; axis < 3; ++axis) {
+        const float ext = cmax[axis] - cmin[axis];
+        if (!(ext > 0.0f) || !std::isfinite(ext)) continue;
+        const float scale = (float)bins / ext;
+        size_t cnt[kBins] = {};
+        float bmn[kBins][3], bmx[kBins][3];
+        for (int b = 0; b < bins; ++b)
+            for (int k = 0; k < 3; ++k) { bmn[b][k] = INFINITY; bmx[b][k] = -INFINITY; }
+        for (size_t i = 0; i < n; ++i) {
+            float mn[3], mx[3];
+            box(items[i], mn, mx);
+            const float c = 0.5f * (mn[axis] + mx[axis]);
+            const int b = std::min(bins - 1, std::max(0, (int)((c - cmin[axis]) * scale)));
+            cnt[b]++;
+            for (int k = 0; k < 3; ++k) {
+                bmn[b][k] = std::min(bmn[b][k], mn[k]);
+                bmx[b][k] = std::max(bmx[b][k], mx[k]);
+            }
+        }
+        // right-to-left suffix areas, then a left-to-right sweep
+        double rarea[kBins];
+        size_t rcnt[kBins];
+        float rmn[3] = {INFINITY, INFINITY, INFINITY}, rmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        size_t rc = 0;
+        for (int b = bins - 1; b >= 1; --b) {
+            for (int k = 0; k < 3; ++k) { rmn[k] = std::min(rmn[k], bmn[b][k]); rmx[k] = std::max(rmx[k], bmx[b][k]); }
+            rc += cnt[b];
+            rarea[b] = area(rmn, rmx);
+            rcnt[b] = rc;
+        }
+        float lmn[3] = {INFINITY, INFINITY, INFINITY}, lmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        size_t lc = 0;
+        for (int b = 1; b < bins; ++b) {   // left = bins [0, b)
+            for (int k = 0; k < 3; ++k) { lmn[k] = std::min(lmn[k], bmn[b - 1][k]); lmx[k] = std::max(lmx[k], bmx[b - 1][k]); }
+            lc += cnt[b - 1];
+            if (lc == 0 || rcnt[b] == 0) continue;
+            const double cost = area(lmn, lmx) * (double)lc + rarea[b] * (double)rcnt[b];
+            if (cost < best_cost) {
+                best_cost = cost;
+                best_axis = axis;
+                best_bin = b;
+            }
+        }
+    }
+    if (best_axis < 0) return n / 2;   // all centroids coincide: any split
+    const float scale = (float)bins / (cmax[best_axis] - cmin[best_axis]);
+    T* mid = std::partition(items, items + n, [&](const T& it) {
+        float mn[3], mx[3];
+        box(it, mn, mx);
+        const float c = 0.5f * (mn[best_axis] + mx[best_axis]);
+        return std::min(bins - 1, std::max(0, (int)((c - cmin[best_axis]) * scale))) < best_bin;
+    });
+    const size_t nl = (size_t)(mid - items);
+    return (nl == 0 || nl == n) ? n / 2 : nl;
+}
+
 // ---- BLAS ------------------------------------------------------------------
 struct MeshTris {
     std::vector<float> v;        // 9 floats per triangle (v0, v1, v2)
@@ -146,6 +229,7 @@ struct BlasJob {
     const MeshTris* tris;
     const uint8_t* axes;   // pre-drawn split axes of this mesh (pre-order)
     orn_bvh_node* out;     // this mesh's node slots (2n-1), post-order
+    bool sah;              // binned-SAH splits instead of the reference's rule
 };
 
 void bbox(const MeshTris& t, const uint32_t* idx, size_t n, float* mn, float* mx) {
@@ -179,13 +263,23 @@ void build_blas(const BlasJob& job, uint32_t* idx, size_t n, size_t node_slot,
         node->node_type = ORN_NODE_TRIANGLE;
         return;
     }
-    const int axis = job.axes[draw];
-    const size_t mid = n / 2;
-    const float* key = t.key.data();
-    std::nth_element(idx, idx + mid, idx + n, [key, axis](uint32_t a, uint32_t b) {
-        float ka = key[(size_t)a * 3 + axis], kb = key[(size_t)b * 3 + axis];
-        return ka < kb || (ka == kb && a < b);
-    });
+    size_t mid = n / 2;
+    if (job.sah) {
+        mid = sah_split(idx, n, [&t](uint32_t i, float* mn, float* mx) {
+            const float* v = &t.v[(size_t)i * 9];
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = std::min(std::min(v[k], v[3 + k]), v[6 + k]);
+                mx[k] = std::max(std::max(v[k], v[3 + k]), v[6 + k]);
+            }
+        });
+    } else {
+        const int axis = job.axes[draw];
+        const float* key = t.key.data();
+        std::nth_element(idx, idx + mid, idx + n, [key, axis](uint32_t a, uint32_t b) {
+            float ka = key[(size_t)a * 3 + axis], kb = key[(size_t)b * 3 + axis];
+            return ka < kb || (ka == kb && a < b);
+        });
+    }
     const size_t nl = mid, nr = n - mid;
     const size_t left_slot = node_slot, right_slot = node_slot + 2 * nl - 1;
     const size_t left_draw = draw + 1, right_draw = draw + 1 + (nl - 1);
@@ -296,9 +390,12 @@ struct TlasBuilder {
             }
     }
 
+    bool sah = false;
+
     // Returns the node for leaves[0..n); the caller appends it.
     orn_bvh_node build(Leaf* leaves, const uint32_t* order, size_t n) {
         if (n == 1) return make_leaf(leaves[0]);
+        if (sah) return build_sah(leaves, n);
         const int axis = axes[draw++];
         const size_t mid = n / 2;
         // sort positions by (aabb.min[axis], original position)
@@ -334,6 +431,32 @@ struct TlasBuilder {
         std::memcpy(node.right_aabb_max_or_v3, rmax, 12);
         node.left_or_custom_id = left_id;
         node.right_or_material_index = right_id;
+        node.node_type = ORN_NODE_INTERNAL;
+        return node;
+    }
+
+    // The non-parity builder: binned-SAH splits over the leaves' boxes.
+    orn_bvh_node build_sah(Leaf* leaves, size_t n) {
+        if (n == 1) return make_leaf(leaves[0]);
+        const size_t mid = sah_split(leaves, n, [](const Leaf& l, float* mn, float* mx) {
+            std::memcpy(mn, l.mn, 12);
+            std::memcpy(mx, l.mx, 12);
+        });
+        orn_bvh_node node;
+        std::memset(&node, 0, sizeof(node));
+        orn_bvh_node left = build_sah(leaves, mid);
+        out->tlas.push_back(left);
+        node.left_or_custom_id = (uint32_t)(out->tlas.size() - 1);
+        orn_bvh_node right = build_sah(leaves + mid, n - mid);
+        out->tlas.push_back(right);
+        node.right_or_material_index = (uint32_t)(out->tlas.size() - 1);
+        float mn[3], mx[3];
+        bounds(leaves, mid, mn, mx);
+        std::memcpy(node.left_aabb_min_or_v0, mn, 12);
+        std::memcpy(node.left_aabb_max_or_v1, mx, 12);
+        bounds(leaves + mid, n - mid, mn, mx);
+        std::memcpy(node.right_aabb_min_or_v2, mn, 12);
+        std::memcpy(node.right_aabb_max_or_v3, mx, 12);
         node.node_type = ORN_NODE_INTERNAL;
         return node;
     }
@@ -453,7 +576,7 @@ int build_all(const orn_scene_desc* d, orn_bvh* b) {
             size_t nt = d->meshes[i].vertex_indices_len / 3;
             std::vector<uint32_t> idx(nt);
             for (size_t k = 0; k < nt; ++k) idx[k] = (uint32_t)k;
-            BlasJob job{&tris[i], axes.data() + draw_base[i], b->blas.data() + blas_base[i]};
+            BlasJob job{&tris[i], axes.data() + draw_base[i], b->blas.data() + blas_base[i], d->builder == ORN_BVH_SAH};
             int spawn = nt > 262144 ? 3 : 0;
             build_blas(job, idx.data(), nt, 0, 0, (uint32_t)blas_base[i], spawn);
         };
@@ -504,6 +627,7 @@ int build_all(const orn_scene_desc* d, orn_bvh* b) {
     tb.mesh_bvh_id = &mesh_bvh_id;
     tb.material_index.assign(d->materials_len, 0xFFFFFFFFu);
     tb.axes = axes.data() + draw_base[M];
+    tb.sah = d->builder == ORN_BVH_SAH;
     b->tlas.reserve(2 * shapes - 1);
     orn_bvh_node root = tb.build(leaves.data(), order.data(), shapes);
     if (tb.status != ORN_OK) return tb.status;

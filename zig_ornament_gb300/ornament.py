@@ -493,8 +493,14 @@ class Bvh:
     ``materials``, ``textures``) and ``blob()`` returns an orn_scene_blob
     pointing at them."""
 
-    def __init__(self, scene: Scene, row_major_transforms: bool = True, seed: int = 1244):
+    def __init__(self, scene: Scene, row_major_transforms: bool = True, seed: int = 1244,
+                 builder: str = "reference"):
+        """builder: "reference" (bvh.zig's rules, the parity tree) or "sah"
+        (binned surface-area heuristic: fewer node visits, not bit-exact
+        with the reference's images)."""
         lib = _lib.load()
+        if builder not in ("reference", "sah"):
+            raise ValueError("builder must be 'reference' or 'sah'")
         mats = {id(m): i for i, m in enumerate(scene.materials)}
         texs = {id(t): i for i, t in enumerate(scene.textures)}
         keep = []
@@ -555,7 +561,8 @@ class Bvh:
                               C.cast(idesc, C.c_void_p), len(scene.mesh_instances),
                               C.cast(mdesc, C.c_void_p), len(scene.materials),
                               C.cast(tdesc, C.c_void_p), len(scene.textures),
-                              seed, 1 if row_major_transforms else 0)
+                              seed, 1 if row_major_transforms else 0,
+                              _lib.BVH_SAH if builder == "sah" else _lib.BVH_REFERENCE)
         handle = C.c_void_p()
         _lib.check(lib.orn_bvh_build(C.byref(desc), C.byref(handle)))
         try:
