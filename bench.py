@@ -431,12 +431,15 @@ def relmse_scene(name, w, h):
     return scenes.instanced_meshes_scene(w, h, n_lights=3)
 
 
-def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8):
+def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=None, warmup=64, methods=None,
+                   ref=None):
     """GPU time each renderer needs to bring the relMSE against an FP64
     `ref_spp`-sample oracle (orn_render_f64) down to `target`: plain
     megakernel tracing, the cached renderer without the network (every pixel
-    traces its full path with light sampling: unbiased) and the cached
-    renderer (its warm-up training frames counted).  Progressive rendering
+    traces its full path with light sampling: unbiased), the cached
+    renderer as configured (lr 1e-3, 64 warm-up training frames counted),
+    and the cached renderer tuned: on the SAH tree (a non-parity tree, like
+    the cached renderer itself), Adam lr 3e-3, 32 warm-up frames.  Progressive rendering
     in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
     chunks outside the timed renders; the crossing is interpolated
     log-linearly between the two chunks around it, or extrapolated as
@@ -446,9 +449,10 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8):
 
     scene = relmse_scene(name, w, h)
     bvh = ornament.Bvh(scene, row_major_transforms=True)
+    bvh_sah = None
 
-    def renderer(kernel):
-        r = ornament.Renderer(bvh, 0)
+    def renderer(kernel, tree=None):
+        r = ornament.Renderer(tree or bvh, 0)
         r.set_resolution(w, h)
         st = ornament.State()
         st.depth = depth
@@ -458,22 +462,31 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8):
         return r, st
 
     t0 = time.time()
-    rr, _ = renderer(_lib.KERNEL_MEGA)
-    ref = rr.render_f64(ref_spp)
-    rr.close()
+    if ref is None:
+        rr, _ = renderer(_lib.KERNEL_MEGA)
+        ref = rr.render_f64(ref_spp)
+        rr.close()
     ref_s = time.time() - t0
     out = {"resolution": f"{w}x{h}", "reference_spp": ref_spp, "reference_seconds": round(ref_s, 1)}
-    for method in ("plain", "light_sampling", "cached"):
+    for method in (methods or ("plain", "light_sampling", "cached", "cached_tuned")):
         kernel = _lib.KERNEL_MEGA if method == "plain" else _lib.KERNEL_CACHED
-        r, st = renderer(kernel)
+        tuned = method == "cached_tuned"
+        if tuned and bvh_sah is None:
+            bvh_sah = ornament.Bvh(scene, row_major_transforms=True, builder="sah")
+        r, st = renderer(kernel, bvh_sah if tuned else None)
         cache = None
         t = 0.0
         if method != "plain":
-            cfg = {"train_shift": 0, "steps_per_frame": 0} if method == "light_sampling" else {"train_shift": 3}
+            if method == "light_sampling":
+                cfg = {"train_shift": 0, "steps_per_frame": 0}
+            elif tuned:
+                cfg = {"train_shift": 3, "learning_rate": 3e-3}
+            else:
+                cfg = cache_cfg or {"train_shift": 3}
             cache = ornament.RadianceCache(seed=1, **cfg)
             r.attach_cache(cache)
-        if method == "cached":
-            st.iterations = 64   # warm-up training frames, then the accumulation restarts
+        if method.startswith("cached"):
+            st.iterations = 32 if tuned else warmup   # warm-up training, then the accumulation restarts
             r.set_state(st.to_struct())
             r.render()
             t += r.last_render_ms() / 1e3
@@ -505,8 +518,10 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8):
         r.close()
         if cache is not None:
             cache.close()
-    out["speedup_cached_vs_plain"] = round(out["plain"]["seconds"] / out["cached"]["seconds"], 3)
-    out["speedup_light_sampling_vs_plain"] = round(out["plain"]["seconds"] / out["light_sampling"]["seconds"], 3)
+    for m in ("cached", "cached_tuned", "light_sampling"):
+        if m in out and "plain" in out:
+            out[f"speedup_{m}_vs_plain"] = round(out["plain"]["seconds"] / out[m]["seconds"], 3)
+    out["_ref"] = ref
     return out
 
 
@@ -516,6 +531,7 @@ def relmse_block(args):
     for name in ("instanced", "closed-room"):
         res["scenes"][name] = time_to_relmse(name, args.relmse_width, args.relmse_height, args.relmse_target,
                                              args.relmse_ref_spp, args.relmse_budget)
+        res["scenes"][name].pop("_ref")
     return res
 
 
