@@ -77,6 +77,7 @@ def parse():
                    help="batch: each frame renders spp/divisor of every scene's 16-256 samples")
     p.add_argument("--tune-cache", default=None, help="batch: autotuner JSON cache (default: none)")
     p.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE block")
+    p.add_argument("--no-sah-line", action="store_true", help="skip the SAH-tree figure")
     p.add_argument("--relmse-width", type=int, default=640)
     p.add_argument("--relmse-height", type=int, default=360)
     p.add_argument("--relmse-target", type=float, default=1e-3)
@@ -403,6 +404,26 @@ def run_ours(args):
                               "visits per ray (profiles/)")},
         "clocks": clocks.summary(),
     }
+    if args.kernel == "mega" and args.bvh == "reference" and not args.no_sah_line:
+        # the same steps on the SAH tree (non-parity mode), for reference
+        try:
+            sah_bvh = ornament.Bvh(scene, builder="sah")
+            rs = ornament.Renderer(sah_bvh, device=local)
+            rs.set_resolution(args.width, args.height)
+            rs.set_state(st)
+            rs.set_camera(scene.camera.to_struct())
+            for _ in range(args.warmup):
+                rs.render()
+            sms = []
+            for _ in range(args.steps):
+                rs.render()
+                sms.append(rs.last_render_ms())
+            line["sah_tree"] = {"value": samples_step / (sum(sms) / len(sms) / 1e3) / 1e6, "unit": UNIT,
+                                "note": "same steps on the binned-SAH tree (orn_scene_desc.builder = SAH): a "
+                                        "non-parity mode, images equal to the reference's in expectation only"}
+            rs.close()
+        except Exception as exc:
+            line["sah_tree"] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.no_relmse and args.kernel == "mega" and args.workload == "instanced" and args.bvh == "reference":
         try:
             line["time_to_relmse"] = relmse_block(args)

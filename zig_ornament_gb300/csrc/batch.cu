@@ -7,11 +7,14 @@
 // space is the concatenation of the contexts' pixels; persistent warps take
 // 32-pixel runs from one counter, so a context with a small frame does not
 // leave the GPU idle while a large one finishes, and one launch replaces one
-// launch (or more) per context.  Every block copies the per-context views
-// (scene pointers, ConstantParams, targets) to shared memory; each lane
-// reads its pixel's view there, so traversal and shading are the
-// megakernel's (pt_machine.cuh, pt_device.cuh) with per-lane scenes, and
-// each pixel's bits equal those of orn_render on its context.
+// launch (or more) per context.  The per-context views (scene pointers,
+// ConstantParams, targets) stay in global memory, read through the L1; a
+// lane keeps its scene's node array and root in registers for traversal and
+// reads the rest of its view when it starts a pixel or shades, so traversal
+// and shading are the megakernel's (pt_machine.cuh, pt_device.cuh) with
+// per-lane scenes, and each pixel's bits equal those of orn_render on its
+// context.  Shared memory holds only the traversal stacks, which leaves the
+// L1 to the node fetches.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -34,23 +37,15 @@ namespace {
 enum BatchLane { B_IDLE = 0, B_TRAVERSE = 1, B_SHADE = 2, B_DONE = 3 };
 
 // Resident blocks per SM each block size is compiled for (80 registers a
-// thread at 128 and 192; the view table and traversal stacks fit in shared
-// memory at these counts).
+// thread at 128 and 192).
 template <int BLOCK> constexpr int batch_min_blocks() { return BLOCK == 64 ? 8 : (BLOCK == 128 ? 6 : 4); }
 
 template <int SEM, bool FAST, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, batch_min_blocks<BLOCK>())
 batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t total_pixels, uint32_t* work_counter,
              uint32_t* error, int shade_threshold) {
-    __shared__ BatchView sv[kMaxBatch];
     __shared__ uint32_t sstack[kSmemStack * BLOCK];
-    {
-        const uint32_t words = nviews * (uint32_t)(sizeof(BatchView) / 4);
-        const uint32_t* src = (const uint32_t*)views;
-        uint32_t* dst = (uint32_t*)sv;
-        for (uint32_t i = threadIdx.x; i < words; i += BLOCK) dst[i] = src[i];
-    }
-    __syncthreads();
+    const BatchView* __restrict__ sv = views;
     TravStack<kSmemStack> stack;
     stack.sstack = sstack + threadIdx.x;
     stack.sstride = BLOCK;
@@ -61,6 +56,12 @@ batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t tota
     int mode = B_IDLE;
     bool exhausted = false;
     uint32_t sc = 0, gid = 0, k = 0, bounce = 0;
+    // the lane's scene as traversal sees it: only the node array and the
+    // root are read by walker_begin / walker_step
+    SceneDev tsc;
+    tsc.nodes = nullptr;
+    tsc.root_ref = 0;
+    tsc.exact_slabs = 0;
     Rng rng{0};
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     f3 ro = mk(0.0f, 0.0f, 0.0f), rd = ro, color = ro;
@@ -84,7 +85,7 @@ batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t tota
             color = mk(1.0f, 1.0f, 1.0f);
             bounce = 0;
             if (V.cp.depth > 0) {
-                walker_begin(w, V.scene, ro, rd);
+                walker_begin(w, tsc, ro, rd);
                 return B_TRAVERSE;
             }
             add_sample(V.cp.current_iteration + (float)k);
@@ -119,6 +120,8 @@ batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t tota
                         else hi = mid - 1u;
                     }
                     sc = lo;
+                    tsc.nodes = sv[sc].scene.nodes;
+                    tsc.root_ref = sv[sc].scene.root_ref;
                     gid = mine - sv[sc].pixel_begin;
                     rng.state = sv[sc].rng[gid];
                     acc = sv[sc].cp.current_iteration > 1.0f ? sv[sc].acc[gid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -133,11 +136,10 @@ batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t tota
             break;
 
         if (mode == B_TRAVERSE) {
-            const BatchView& V = sv[sc];
+            const float t_min = sv[sc].cp.ray_cast_epsilon;
 #pragma unroll 1
             for (int s = 0; s < kStepsPerIteration; ++s) {
-                if (!walker_step<false, kSmemStack, FAST>(w, V.scene, ro, rd, V.cp.ray_cast_epsilon, &h, stack, &vc,
-                                                          &err)) {
+                if (!walker_step<false, kSmemStack, FAST>(w, tsc, ro, rd, t_min, &h, stack, &vc, &err)) {
                     mode = B_SHADE;
                     break;
                 }
@@ -158,7 +160,7 @@ batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t tota
                     cont = shade_hit<SEM, MATH_PORTABLE, false>(V.scene, V.cp, rng, h, &ro, &rd, &color, &scn);
                 }
                 if (cont && ++bounce < V.cp.depth) {
-                    walker_begin(w, V.scene, ro, rd);
+                    walker_begin(w, tsc, ro, rd);
                     mode = B_TRAVERSE;
                 } else {
                     add_sample(V.cp.current_iteration + (float)k);
