@@ -175,7 +175,15 @@ typedef struct orn_state {
     uint32_t semantics;       /* enum orn_semantics, default HIP */
     uint32_t kernel;          /* enum orn_kernel, default MEGA   */
     uint32_t spp_per_launch;  /* 0 = library chooses             */
+    uint32_t triangle_test;   /* enum orn_triangle_test, default MOLLER_TRUMBORE */
 } orn_state;
+
+/* Ray/triangle test.  MOLLER_TRUMBORE is the reference's (bvh.hip.h:72-117),
+ * the one every parity claim is made on.  WATERTIGHT (no counterpart in the
+ * reference) is Woop, Benthin and Wald's watertight test: a ray through an
+ * edge or vertex shared by two triangles of a mesh always hits one of them;
+ * results can differ from the reference's at such edges. */
+enum orn_triangle_test { ORN_TRIANGLE_MOLLER_TRUMBORE = 0, ORN_TRIANGLE_WATERTIGHT = 1 };
 
 /* A ray for orn_trace_rays (src/hip_backend/kernels/ray.hip.h:7-18). */
 typedef struct orn_ray {

@@ -34,6 +34,7 @@ CACHE_PARAM_COUNT = 33792
 KERNEL_CACHED = 2
 BATCH_MAX = 64
 BVH_REFERENCE, BVH_SAH = 0, 1
+TRIANGLE_MOLLER_TRUMBORE, TRIANGLE_WATERTIGHT = 0, 1
 COUNTER_NAMES = ["samples", "rays", "visits", "internal", "sphere_leaf", "mesh_entry", "triangle",
                  "sphere_hits", "mesh_hits", "textured_hits"]
 
@@ -91,7 +92,8 @@ class SceneBlob(C.Structure):
 class State(C.Structure):
     _fields_ = [("depth", C.c_uint32), ("flip_y", C.c_uint32), ("inverted_gamma", C.c_float),
                 ("iterations", C.c_uint32), ("ray_cast_epsilon", C.c_float),
-                ("semantics", C.c_uint32), ("kernel", C.c_uint32), ("spp_per_launch", C.c_uint32)]
+                ("semantics", C.c_uint32), ("kernel", C.c_uint32), ("spp_per_launch", C.c_uint32),
+                ("triangle_test", C.c_uint32)]
 
 
 class Ray(C.Structure):

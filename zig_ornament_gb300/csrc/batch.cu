@@ -56,12 +56,13 @@ batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t tota
     int mode = B_IDLE;
     bool exhausted = false;
     uint32_t sc = 0, gid = 0, k = 0, bounce = 0;
-    // the lane's scene as traversal sees it: only the node array and the
-    // root are read by walker_begin / walker_step
+    // the lane's scene as traversal sees it: walker_begin / walker_step read
+    // only the node array, the root and the triangle-test choice
     SceneDev tsc;
     tsc.nodes = nullptr;
     tsc.root_ref = 0;
     tsc.exact_slabs = 0;
+    tsc.watertight = 0;
     Rng rng{0};
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     f3 ro = mk(0.0f, 0.0f, 0.0f), rd = ro, color = ro;
@@ -122,6 +123,7 @@ batch_kernel(const BatchView* __restrict__ views, uint32_t nviews, uint32_t tota
                     sc = lo;
                     tsc.nodes = sv[sc].scene.nodes;
                     tsc.root_ref = sv[sc].scene.root_ref;
+                    tsc.watertight = sv[sc].scene.watertight;
                     gid = mine - sv[sc].pixel_begin;
                     rng.state = sv[sc].rng[gid];
                     acc = sv[sc].cp.current_iteration > 1.0f ? sv[sc].acc[gid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);

@@ -300,10 +300,12 @@ void relayout_nodes(const orn_scene_blob* b, std::vector<float4>* out) {
                 o[3] = make_float4(e[0], e[1], e[2], 0.0f);
                 break;
             case ORN_NODE_TRIANGLE:
-                // e1 = v1 - v0, e2 = v2 - v0: the subtractions of bvh.hip.h:81-82
+                // the vertices as given (the test subtracts them on the fly,
+                // bvh.hip.h:81-82), so triangles sharing an edge see the same
+                // floats (the watertight test relies on it)
                 o[0] = make_float4(a[0], a[1], a[2], u2f(n.left_or_custom_id));
-                o[1] = make_float4(bb[0] - a[0], bb[1] - a[1], bb[2] - a[2], 0.0f);
-                o[2] = make_float4(c[0] - a[0], c[1] - a[1], c[2] - a[2], u2f(ORN_NODE_TRIANGLE));
+                o[1] = make_float4(bb[0], bb[1], bb[2], 0.0f);
+                o[2] = make_float4(c[0], c[1], c[2], u2f(ORN_NODE_TRIANGLE));
                 o[3] = make_float4(0, 0, 0, 0);
                 break;
             default: {  // sphere / mesh leaf: inverse rows 0..2 inline
@@ -861,9 +863,11 @@ int orn_destroy(orn_context* ctx) {
 
 int orn_set_state(orn_context* ctx, const orn_state* s) {
     if (!ctx || !s) return ORN_ERR_INVALID_ARGUMENT;
-    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED)
-        return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics or kernel");
+    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED ||
+        s->triangle_test > ORN_TRIANGLE_WATERTIGHT)
+        return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics, kernel or triangle test");
     ctx->state = *s;
+    ctx->scene.watertight = s->triangle_test == ORN_TRIANGLE_WATERTIGHT ? 1u : 0u;
     return ORN_OK;
 }
 

@@ -159,6 +159,81 @@ __device__ __forceinline__ bool slab_safe(f3 o) {
     return fabsf(o.x) < 1e30f && fabsf(o.y) < 1e30f && fabsf(o.z) < 1e30f;
 }
 
+// Möller–Trumbore exactly as bvh.hip.h:72-117 (e1 = v1 - v0, e2 = v2 - v0):
+// true when the hit distance t satisfies t_min <= t < t_max; (u, v) are the
+// weights of v1 and v2.
+__device__ __forceinline__ bool tri_mt(f3 o, f3 d, f3 v0, f3 v1, f3 v2, float t_min, float t_max, float* t_out,
+                                       float* u_out, float* v_out) {
+    const f3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    const f3 s1 = cross(d, e2);
+    const float det = dot(s1, e1);
+    const float invd = 1.0f / det;
+    const f3 dd = sub(o, v0);
+    const float u = dot(dd, s1) * invd;
+    if (u < 0.0f || u > 1.0f) return false;
+    const f3 s2 = cross(dd, e1);
+    const float v = dot(d, s2) * invd;
+    if (v < 0.0f || u + v > 1.0f) return false;
+    const float t = dot(e2, s2) * invd;
+    if (t < t_min || t > t_max || !(t < t_max)) return false;
+    *t_out = t;
+    *u_out = u;
+    *v_out = v;
+    return true;
+}
+
+__device__ __forceinline__ float comp(f3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+// Watertight ray/triangle test (Woop, Benthin, Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2013): the ray is sheared so that it runs along +z
+// from the origin, the triangle's 2-D edge functions U, V, W decide the hit
+// (recomputed in double when one is exactly zero), so a ray through an edge
+// or vertex shared by two triangles hits at least one of them.  Same
+// acceptance rule and (u, v) meaning as tri_mt.  A non-parity option: it
+// can decide edge cases differently from the reference's test.  Kept out of
+// line so the reference test's path through the traversal loop keeps its
+// registers.
+static __device__ __noinline__ bool tri_watertight(f3 o, f3 d, f3 v0, f3 v1, f3 v2, float t_min, float t_max,
+                                               float* t_out, float* u_out, float* v_out) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1, ky = kx == 2 ? 0 : kx + 1;
+    const float dz = comp(d, kz);
+    if (dz < 0.0f) {
+        const int tmp = kx;
+        kx = ky;
+        ky = tmp;
+    }
+    const float sx = comp(d, kx) / dz, sy = comp(d, ky) / dz, sz = 1.0f / dz;
+    const f3 A = sub(v0, o), B = sub(v1, o), C = sub(v2, o);
+    const float Ax = comp(A, kx) - sx * comp(A, kz), Ay = comp(A, ky) - sy * comp(A, kz);
+    const float Bx = comp(B, kx) - sx * comp(B, kz), By = comp(B, ky) - sy * comp(B, kz);
+    const float Cx = comp(C, kx) - sx * comp(C, kz), Cy = comp(C, ky) - sy * comp(C, kz);
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = U + V + W;
+    if (det == 0.0f) return false;
+    float T = U * (sz * comp(A, kz)) + V * (sz * comp(B, kz)) + W * (sz * comp(C, kz));
+    if (det < 0.0f) {
+        det = -det;
+        T = -T;
+        V = -V;
+        W = -W;
+    }
+    const float rcp = 1.0f / det;
+    const float t = T * rcp;
+    if (t < t_min || t > t_max || !(t < t_max)) return false;
+    *t_out = t;
+    *u_out = V * rcp;
+    *v_out = W * rcp;
+    return true;
+}
+
 struct HitRec {
     float t;
     uint32_t material;
@@ -244,30 +319,20 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
             }
         } else if (type == ORN_NODE_TRIANGLE) {
             if (COUNT) vc->tri++;
-            // Möller–Trumbore exactly as bvh.hip.h:72-117 (e1, e2 precomputed)
-            f3 v1 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
-            f3 s1 = cross(d, e2);
-            float det = dot(s1, e1);
-            float invd = 1.0f / det;
-            f3 dd = sub(o, v1);
-            float u = dot(dd, s1) * invd;
-            if (!(u < 0.0f || u > 1.0f)) {
-                f3 s2 = cross(dd, e1);
-                float v = dot(d, s2) * invd;
-                if (!(v < 0.0f || u + v > 1.0f)) {
-                    float t = dot(e2, s2) * invd;
-                    if (!(t < t_min || t > t_max) && t < t_max) {
-                        any = true;
-                        t_max = t;
-                        out->t = t;
-                        out->material = material;
-                        out->type = ORN_NODE_MESH;
-                        out->inv = inv_id;
-                        out->tri = bits(a.w) * 3u;
-                        out->u = u;
-                        out->v = v;
-                    }
-                }
+            const f3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+            float t, u, v;
+            const bool hit = sc.watertight ? tri_watertight(o, d, v0, v1, v2, t_min, t_max, &t, &u, &v)
+                                           : tri_mt(o, d, v0, v1, v2, t_min, t_max, &t, &u, &v);
+            if (hit) {
+                any = true;
+                t_max = t;
+                out->t = t;
+                out->material = material;
+                out->type = ORN_NODE_MESH;
+                out->inv = inv_id;
+                out->tri = bits(a.w) * 3u;
+                out->u = u;
+                out->v = v;
             }
         } else if (type == ORN_NODE_SPHERE || type == ORN_NODE_MESH) {
             // inverse rows 0..2: a, b, (c.xyz, e.x)

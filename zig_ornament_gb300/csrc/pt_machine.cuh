@@ -107,29 +107,20 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
         ldg8(np, &a, &b);
         ldg8(np + 2, &c, &e);
         (void)e;
-        f3 v1 = mk(a.x, a.y, a.z), e1 = mk(b.x, b.y, b.z), e2 = mk(c.x, c.y, c.z);
-        f3 s1 = cross(w.d, e2);
-        float det = dot(s1, e1);
-        float invd = 1.0f / det;
-        f3 dd = sub(w.o, v1);
-        float u = dot(dd, s1) * invd;
-        if (!(u < 0.0f || u > 1.0f)) {
-            f3 s2 = cross(dd, e1);
-            float v = dot(w.d, s2) * invd;
-            if (!(v < 0.0f || u + v > 1.0f)) {
-                float t = dot(e2, s2) * invd;
-                if (!(t < t_min || t > w.t_max) && t < w.t_max) {
-                    w.any = true;
-                    w.t_max = t;
-                    out->t = t;
-                    out->material = w.material;
-                    out->type = ORN_NODE_MESH;
-                    out->inv = w.inv_id;
-                    out->tri = bits(a.w) * 3u;
-                    out->u = u;
-                    out->v = v;
-                }
-            }
+        const f3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+        float t, u, v;
+        const bool hit = sc.watertight ? tri_watertight(w.o, w.d, v0, v1, v2, t_min, w.t_max, &t, &u, &v)
+                                       : tri_mt(w.o, w.d, v0, v1, v2, t_min, w.t_max, &t, &u, &v);
+        if (hit) {
+            w.any = true;
+            w.t_max = t;
+            out->t = t;
+            out->material = w.material;
+            out->type = ORN_NODE_MESH;
+            out->inv = w.inv_id;
+            out->tri = bits(a.w) * 3u;
+            out->u = u;
+            out->v = v;
         }
     } else {
         float4 a, b, c, e;

@@ -48,6 +48,7 @@ struct SceneDev {
     const float4* materials;    // 2 float4 per material
     const TexDesc* textures;
     uint32_t textures_len;
+    uint32_t watertight;        // 1: watertight triangle test (orn_state.triangle_test), 0: the reference's
 };
 
 }  // namespace orn

@@ -294,6 +294,7 @@ class State:
         self.semantics = _lib.SEMANTICS_HIP
         self.kernel = _lib.KERNEL_MEGA
         self.spp_per_launch = 0
+        self.triangle_test = _lib.TRIANGLE_MOLLER_TRUMBORE
 
     def setFlipY(self, v): self.flip_y = bool(v)
     def getFlipY(self): return self.flip_y
@@ -320,6 +321,7 @@ class State:
         s.semantics = self.semantics
         s.kernel = self.kernel
         s.spp_per_launch = self.spp_per_launch
+        s.triangle_test = self.triangle_test
         return s
 
 
