@@ -45,6 +45,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Msamples/s at 1080p"
 UNIT = "Msamples/s"
+TREE_SUFFIX = {"reference": "", "sah": ", SAH tree", "lbvh": ", LBVH tree"}
+TREE_DESC = {"reference": "bvh.zig rules (random axis, median split): the parity tree",
+             "sah": "binned SAH (non-parity mode)",
+             "lbvh": "GPU-built linear BVH BLASes + SAH TLAS (non-parity mode)"}
 
 
 def parse():
@@ -57,9 +61,10 @@ def parse():
                    help="instanced: the 1080p instanced-mesh scene (default, the headline); spheres: the "
                         "640x360 sphere field (64 spp, depth 10); large: 4096 instances over ~10M "
                         "triangles at 3840x2160 (depth 16)")
-    p.add_argument("--bvh", default="reference", choices=["reference", "sah"],
-                   help="reference: bvh.zig's tree (the parity tree, default); sah: the binned-SAH tree "
-                        "(non-parity mode: fewer node visits, images equal in expectation)")
+    p.add_argument("--bvh", default="reference", choices=["reference", "sah", "lbvh"],
+                   help="reference: bvh.zig's tree (the parity tree, default); sah: the binned-SAH tree; "
+                        "lbvh: BLASes built on the GPU as linear BVHs, TLAS by SAH (both non-parity modes: "
+                        "fewer node visits, images equal in expectation)")
     p.add_argument("--spp", type=int, default=None, help="sample passes per step (render iterations)")
     p.add_argument("--width", type=int, default=None)
     p.add_argument("--height", type=int, default=None)
@@ -105,7 +110,7 @@ def apply_workload_defaults(args):
 def metric_name(args):
     if args.workload == "instanced" and (args.width, args.height) == (1920, 1080) and args.bvh == "reference":
         return METRIC
-    return f"Msamples/s, {args.workload} {args.width}x{args.height}" + (", SAH tree" if args.bvh == "sah" else "")
+    return f"Msamples/s, {args.workload} {args.width}x{args.height}" + TREE_SUFFIX[args.bvh]
 
 
 def workload(args):
@@ -123,10 +128,11 @@ def workload(args):
         scene = scenes.instanced_meshes_scene(args.width, args.height)
         desc = ("instanced meshes TLAS/BLAS: 8 BLAS icospheres+tori 10k-80k tris, 256 instances, "
                 "4 procedural 1024^2 RGBA8 textures, 1 emissive quad (radiance 15)")
+    t_build = time.perf_counter()
     bvh = ornament.Bvh(scene, builder=args.bvh)
+    t_build = time.perf_counter() - t_build
     tris = sum(len(m.vertex_indices) // 3 for m in scene.meshes)
-    cfg = {"workload": desc, "bvh": ("bvh.zig rules (random axis, median split): the parity tree"
-                                     if args.bvh == "reference" else "binned SAH (non-parity mode)"),
+    cfg = {"workload": desc, "bvh": TREE_DESC[args.bvh], "bvh_build_s": round(t_build, 3),
            "resolution": f"{args.width}x{args.height}", "spp_per_step": args.spp, "depth": args.depth,
            "triangles": tris, "instances": len(scene.mesh_instances), "blas": len(scene.meshes),
            "tlas_nodes": int(len(bvh.tlas_nodes)), "blas_nodes": int(len(bvh.blas_nodes)),
@@ -405,25 +411,30 @@ def run_ours(args):
         "clocks": clocks.summary(),
     }
     if args.kernel == "mega" and args.bvh == "reference" and not args.no_sah_line:
-        # the same steps on the SAH tree (non-parity mode), for reference
-        try:
-            sah_bvh = ornament.Bvh(scene, builder="sah")
-            rs = ornament.Renderer(sah_bvh, device=local)
-            rs.set_resolution(args.width, args.height)
-            rs.set_state(st)
-            rs.set_camera(scene.camera.to_struct())
-            for _ in range(args.warmup):
-                rs.render()
-            sms = []
-            for _ in range(args.steps):
-                rs.render()
-                sms.append(rs.last_render_ms())
-            line["sah_tree"] = {"value": samples_step / (sum(sms) / len(sms) / 1e3) / 1e6, "unit": UNIT,
-                                "note": "same steps on the binned-SAH tree (orn_scene_desc.builder = SAH): a "
-                                        "non-parity mode, images equal to the reference's in expectation only"}
-            rs.close()
-        except Exception as exc:
-            line["sah_tree"] = {"error": f"{type(exc).__name__}: {exc}"}
+        # the same steps on the non-parity trees, for reference
+        for alt in ("sah", "lbvh"):
+            key = alt + "_tree"
+            try:
+                t_alt = time.perf_counter()
+                alt_bvh = ornament.Bvh(scene, builder=alt)
+                t_alt = time.perf_counter() - t_alt
+                rs = ornament.Renderer(alt_bvh, device=local)
+                rs.set_resolution(args.width, args.height)
+                rs.set_state(st)
+                rs.set_camera(scene.camera.to_struct())
+                for _ in range(args.warmup):
+                    rs.render()
+                sms = []
+                for _ in range(args.steps):
+                    rs.render()
+                    sms.append(rs.last_render_ms())
+                line[key] = {"value": samples_step / (sum(sms) / len(sms) / 1e3) / 1e6, "unit": UNIT,
+                             "bvh_build_s": round(t_alt, 3),
+                             "note": f"same steps on the {TREE_DESC[alt]} tree: images equal to the "
+                                     "reference's in expectation only"}
+                rs.close()
+            except Exception as exc:
+                line[key] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.no_relmse and args.kernel == "mega" and args.workload == "instanced" and args.bvh == "reference":
         try:
             line["time_to_relmse"] = relmse_block(args)

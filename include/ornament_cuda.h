@@ -532,7 +532,12 @@ typedef struct orn_scene_desc {
  * unchanged with fewer node visits; images agree with the reference's in
  * expectation, not bit for bit (equal-distance hits may resolve to another
  * primitive and visit counts differ). */
-enum orn_bvh_builder { ORN_BVH_REFERENCE = 0, ORN_BVH_SAH = 1 };
+enum orn_bvh_builder { ORN_BVH_REFERENCE = 0, ORN_BVH_SAH = 1, ORN_BVH_LBVH = 2 };
+/* LBVH (no counterpart in the reference): the BLASes are built on the GPU
+ * (device 0 or the current device) as linear BVHs — Morton-code sort and
+ * Karras' hierarchy, far faster to build than the CPU builders, fewer visits
+ * than the reference's tree, more than SAH — and the TLAS with SAH on the
+ * CPU.  Needs a CUDA device; non-parity like SAH. */
 
 typedef struct orn_bvh orn_bvh;
 

@@ -33,7 +33,7 @@ CACHE_OUTPUTS = 3
 CACHE_PARAM_COUNT = 33792
 KERNEL_CACHED = 2
 BATCH_MAX = 64
-BVH_REFERENCE, BVH_SAH = 0, 1
+BVH_REFERENCE, BVH_SAH, BVH_LBVH = 0, 1, 2
 TRIANGLE_MOLLER_TRUMBORE, TRIANGLE_WATERTIGHT = 0, 1
 COUNTER_NAMES = ["samples", "rays", "visits", "internal", "sphere_leaf", "mesh_entry", "triangle",
                  "sphere_hits", "mesh_hits", "textured_hits"]

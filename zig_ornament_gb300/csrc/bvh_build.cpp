@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "ornament_cuda.h"
+#include "lbvh.h"
 
 static_assert(sizeof(orn_bvh_node) == 64, "BvhNode is 64 bytes");
 static_assert(sizeof(orn_material) == 32, "Material is 32 bytes");
@@ -466,6 +467,7 @@ int validate(const orn_scene_desc* d) {
     if (!d) return ORN_ERR_INVALID_ARGUMENT;
     uint64_t shapes = (uint64_t)d->spheres_len + d->meshes_len + d->mesh_instances_len;
     if (shapes == 0) return ORN_ERR_EMPTY_SCENE;
+    if (d->builder > ORN_BVH_LBVH) return ORN_ERR_INVALID_ARGUMENT;
     if ((d->spheres_len && !d->spheres) || (d->meshes_len && !d->meshes) ||
         (d->mesh_instances_len && !d->mesh_instances) ||
         (d->materials_len && !d->materials) || (d->textures_len && !d->textures))
@@ -585,6 +587,16 @@ int build_all(const orn_scene_desc* d, orn_bvh* b) {
         std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) {
             return d->meshes[a].vertex_indices_len > d->meshes[c].vertex_indices_len;
         });
+        if (d->builder == ORN_BVH_LBVH) {
+            // on the GPU, one mesh after another
+            for (uint32_t i = 0; i < M; ++i) {
+                const size_t nt = d->meshes[i].vertex_indices_len / 3;
+                int st = orn::lbvh_build_blas(tris[i].v.data(), (uint32_t)nt, tris[i].first_global,
+                                              (uint32_t)blas_base[i], b->blas.data() + blas_base[i]);
+                if (st != ORN_OK) return st;
+            }
+            order.clear();
+        }
         std::atomic_size_t cursor{0};
         unsigned nthreads = std::min<unsigned>(hw, std::max<uint32_t>(1, M));
         for (unsigned w = 0; w < nthreads; ++w)
@@ -627,7 +639,7 @@ int build_all(const orn_scene_desc* d, orn_bvh* b) {
     tb.mesh_bvh_id = &mesh_bvh_id;
     tb.material_index.assign(d->materials_len, 0xFFFFFFFFu);
     tb.axes = axes.data() + draw_base[M];
-    tb.sah = d->builder == ORN_BVH_SAH;
+    tb.sah = d->builder == ORN_BVH_SAH || d->builder == ORN_BVH_LBVH;
     b->tlas.reserve(2 * shapes - 1);
     orn_bvh_node root = tb.build(leaves.data(), order.data(), shapes);
     if (tb.status != ORN_OK) return tb.status;

@@ -497,12 +497,13 @@ class Bvh:
 
     def __init__(self, scene: Scene, row_major_transforms: bool = True, seed: int = 1244,
                  builder: str = "reference"):
-        """builder: "reference" (bvh.zig's rules, the parity tree) or "sah"
-        (binned surface-area heuristic: fewer node visits, not bit-exact
-        with the reference's images)."""
+        """builder: "reference" (bvh.zig's rules, the parity tree), "sah"
+        (binned surface-area heuristic on the CPU) or "lbvh" (linear BVHs
+        built on the GPU); the last two give fewer node visits and are not
+        bit-exact with the reference's images."""
         lib = _lib.load()
-        if builder not in ("reference", "sah"):
-            raise ValueError("builder must be 'reference' or 'sah'")
+        if builder not in ("reference", "sah", "lbvh"):
+            raise ValueError("builder must be 'reference', 'sah' or 'lbvh'")
         mats = {id(m): i for i, m in enumerate(scene.materials)}
         texs = {id(t): i for i, t in enumerate(scene.textures)}
         keep = []
@@ -564,7 +565,8 @@ class Bvh:
                               C.cast(mdesc, C.c_void_p), len(scene.materials),
                               C.cast(tdesc, C.c_void_p), len(scene.textures),
                               seed, 1 if row_major_transforms else 0,
-                              _lib.BVH_SAH if builder == "sah" else _lib.BVH_REFERENCE)
+                              {"reference": _lib.BVH_REFERENCE, "sah": _lib.BVH_SAH,
+                               "lbvh": _lib.BVH_LBVH}[builder])
         handle = C.c_void_p()
         _lib.check(lib.orn_bvh_build(C.byref(desc), C.byref(handle)))
         try:
