@@ -41,7 +41,9 @@ enum orn_status {
     ORN_ERR_BAD_SCENE = 6,        /* an index in the scene is out of range  */
     ORN_ERR_STACK_OVERFLOW = 7,   /* a ray needed more than 64 stack slots  */
     ORN_ERR_BUFFER_TOO_SMALL = 8, /* destination smaller than the target    */
-    ORN_ERR_TIMEOUT = 9           /* a bounded device-side wait gave up     */
+    ORN_ERR_TIMEOUT = 9,          /* a bounded device-side wait gave up     */
+    ORN_ERR_UNSUPPORTED = 10,     /* valid input of a kind not handled      */
+    ORN_ERR_BAD_IMAGE = 11        /* a corrupt or truncated image stream    */
 };
 
 /* ---- GPU data layouts (src/gpu_structs.zig) ---------------------------- */
@@ -549,6 +551,36 @@ int orn_bvh_build(const orn_scene_desc* desc, orn_bvh** out);
 int orn_bvh_get_blob(const orn_bvh* bvh, orn_scene_blob* blob);
 /* Bvh.deinit — src/bvh.zig:80-90. */
 int orn_bvh_free(orn_bvh* bvh);
+
+/* ---- JPEG textures -------------------------------------------------------
+ * The example app loads its textures with zstbi (stb_image) as 4-component
+ * RGBA8 images flipped vertically on load (glfw_example/examples.zig:492-503
+ * loadTexture(..., 4); glfw_example/app_no_interop.zig:17
+ * setFlipVerticallyOnLoad(true)) and passes them to Scene.createTexture
+ * (src/scene.zig:339-351).  These calls replace that loader for JPEG files:
+ * sequential Huffman JPEG (SOF0/SOF1, 8-bit, 1 or 3 components, any 1..4
+ * sampling factors, restart intervals); progressive, arithmetic-coded,
+ * lossless, 12-bit and CMYK streams return ORN_ERR_UNSUPPORTED, corrupt
+ * ones ORN_ERR_BAD_IMAGE.  Entropy decoding runs on the host; dequantisation,
+ * the inverse DCT (exact, FP32), chroma replication, YCbCr->RGB and the flip
+ * run on the GPU.  Outputs may differ from stb_image's by a few levels (its
+ * integer IDCT and chroma filter are not reproduced). */
+
+/* Width, height and component count from the frame header (host only). */
+int orn_jpeg_info(const void* data, size_t len, uint32_t* width, uint32_t* height, uint32_t* components);
+/* Decodes into `rgba` (width * height * 4 bytes, row-major, alpha 255) on
+ * `device` (-1: the current device); flip_y = 1 puts the last image row
+ * first, like stb_image's flip-on-load.  Synchronous. */
+int orn_jpeg_decode(const void* data, size_t len, int device, uint32_t flip_y, uint8_t* rgba, size_t rgba_len);
+/* Parity / debugging (host only): the quantised coefficients of one
+ * component as entropy-decoded, [blocks_h][blocks_w][64] in natural
+ * (row-major) order, the planes padded to whole MCUs, and the component's
+ * quantisation table (64 values, natural order).  `out` may be null to query
+ * the plane size; any of blocks_w, blocks_h and quant may be null. */
+int orn_jpeg_coefficients(const void* data, size_t len, uint32_t component, int16_t* out, size_t out_len,
+                          uint32_t* blocks_w, uint32_t* blocks_h, uint16_t* quant);
+/* Message of the calling thread's last failed orn_jpeg_* call. */
+const char* orn_jpeg_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ ORN_OK = 0
 STATUS_NAMES = {
     0: "ORN_OK", 1: "ORN_ERR_INVALID_ARGUMENT", 2: "ORN_ERR_EMPTY_SCENE", 3: "ORN_ERR_OUT_OF_MEMORY",
     4: "ORN_ERR_CUDA", 5: "ORN_ERR_NO_DEVICE", 6: "ORN_ERR_BAD_SCENE", 7: "ORN_ERR_STACK_OVERFLOW",
-    8: "ORN_ERR_BUFFER_TOO_SMALL", 9: "ORN_ERR_TIMEOUT",
+    8: "ORN_ERR_BUFFER_TOO_SMALL", 9: "ORN_ERR_TIMEOUT", 10: "ORN_ERR_UNSUPPORTED", 11: "ORN_ERR_BAD_IMAGE",
 }
 NODE_INTERNAL, NODE_SPHERE, NODE_MESH, NODE_TRIANGLE = 0, 1, 2, 3
 LAMBERTIAN, METAL, DIELECTRIC, DIFFUSE_LIGHT = 0, 1, 2, 3
@@ -210,6 +210,12 @@ FUNCTIONS = {
     "orn_bvh_build": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "orn_bvh_get_blob": (C.c_int, [_P, C.POINTER(SceneBlob)]),
     "orn_bvh_free": (C.c_int, [_P]),
+    "orn_jpeg_info": (C.c_int, [_P, C.c_size_t, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                C.POINTER(C.c_uint32)]),
+    "orn_jpeg_decode": (C.c_int, [_P, C.c_size_t, C.c_int, C.c_uint32, _P, C.c_size_t]),
+    "orn_jpeg_coefficients": (C.c_int, [_P, C.c_size_t, C.c_uint32, _P, C.c_size_t, C.POINTER(C.c_uint32),
+                                        C.POINTER(C.c_uint32), _P]),
+    "orn_jpeg_last_error": (C.c_char_p, []),
 }
 
 _lib = None

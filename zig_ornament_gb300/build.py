@@ -63,18 +63,18 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     cu, cpp = _sources()
     jobs = []
     for src in cu:
-        obj = BUILD / (src.stem + ".o")
+        obj = BUILD / (src.name + ".o")
         extra = ["-Xptxas", "-v"] if verbose else []
         jobs.append([nvcc, *NVCC_FLAGS, *ARCH, *extra, "-c", str(src), "-o", str(obj)])
     for src in cpp:
-        obj = BUILD / (src.stem + ".o")
+        obj = BUILD / (src.name + ".o")
         jobs.append(["g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    objs = [str(BUILD / (s.stem + ".o")) for s in cu + cpp]
+    objs = [str(BUILD / (s.name + ".o")) for s in cu + cpp]
     tmp = LIB.with_suffix(".so.tmp")
     _run([nvcc, "-shared", *ARCH, "-o", str(tmp), *objs, "-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, LIB)

@@ -678,6 +678,8 @@ const char* orn_status_string(int status) {
         case ORN_ERR_STACK_OVERFLOW: return "traversal stack overflow";
         case ORN_ERR_BUFFER_TOO_SMALL: return "buffer too small";
         case ORN_ERR_TIMEOUT: return "device-side limit reached";
+        case ORN_ERR_UNSUPPORTED: return "unsupported input";
+        case ORN_ERR_BAD_IMAGE: return "corrupt image data";
         default: return "unknown status";
     }
 }
