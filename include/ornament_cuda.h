@@ -178,7 +178,18 @@ typedef struct orn_state {
     uint32_t kernel;          /* enum orn_kernel, default MEGA   */
     uint32_t spp_per_launch;  /* 0 = library chooses             */
     uint32_t triangle_test;   /* enum orn_triangle_test, default MOLLER_TRUMBORE */
+    uint32_t pixel_order;     /* enum orn_pixel_order, default COST */
 } orn_state;
+
+/* Order in which a plain megakernel launch (ORN_KERNEL_MEGA, and
+ * orn_render_f64) hands pixels to lanes (no counterpart in the reference,
+ * whose grid is one thread per pixel).  Results are the same either way.
+ * COST: from the second launch of a context on, tiles of 32 pixels go out
+ * costliest first, by the traversal steps they took in the previous launch,
+ * so that the launch does not end with a few lanes finishing expensive
+ * pixels; RASTER: pixel index order.  The cached kernel (one sample per
+ * pixel per launch, costs too noisy to predict) always uses raster order. */
+enum orn_pixel_order { ORN_PIXEL_ORDER_COST = 0, ORN_PIXEL_ORDER_RASTER = 1 };
 
 /* Ray/triangle test.  MOLLER_TRUMBORE is the reference's (bvh.hip.h:72-117),
  * the one every parity claim is made on.  WATERTIGHT (no counterpart in the

@@ -366,3 +366,35 @@ def test_sah_tree_renders_like_the_oracle(oracle, kernel):
     assert np.array_equal(rng, orng)
     assert np.array_equal(bits(acc), bits(oacc))
     r.close()
+
+
+@pytest.mark.parametrize("kernel", [_lib.KERNEL_MEGA, _lib.KERNEL_CACHED], ids=["mega", "cached"])
+def test_pixel_order_does_not_change_results(kernel):
+    """Longest-first hand-out (orn_state.pixel_order = COST, the default)
+    against raster order over several launches: the same bits."""
+    scene = scenes.instanced_meshes_scene(96, 54, seed=1, n_blas=4, n_instances=40, tri_range=(2000, 8000),
+                                          texture_size=64, n_lights=3)
+    bvh = ornament.Bvh(scene)
+    outs = []
+    for order in (_lib.PIXEL_ORDER_RASTER, _lib.PIXEL_ORDER_COST):
+        r = ornament.Renderer(bvh, device=0)
+        cache = None
+        if kernel == _lib.KERNEL_CACHED:
+            # no training steps: float atomics in the weight-gradient sums
+            # make trained weights differ in the last bits between runs
+            cache = ornament.RadianceCache(seed=1, train_shift=3, steps_per_frame=0)
+            r.attach_cache(cache)
+        r.set_resolution(96, 54)
+        st = make_state(depth=8, iterations=6, spp_per_launch=2, kernel=kernel)
+        st.pixel_order = order
+        r.set_state(st)
+        r.set_camera(scene.camera.to_struct())
+        r.render()
+        r.render()
+        acc, rng, _ = r.progress()
+        outs.append((bits(acc), rng))
+        r.close()
+        if cache is not None:
+            cache.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])

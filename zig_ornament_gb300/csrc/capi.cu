@@ -53,6 +53,14 @@ struct orn_context {
     float4* acc = nullptr;
     float4* fb = nullptr;
     uint32_t* rng = nullptr;
+    // longest-first pixel order (order.cu): per-pixel costs of the last
+    // launch, the order derived from them, and the sort's buffers
+    uint32_t* px_cost = nullptr;
+    uint32_t* px_order = nullptr;
+    uint32_t* tile_buf = nullptr;     // 4 arrays of one entry per tile
+    void* sort_temp = nullptr;
+    size_t sort_temp_bytes = 0;
+    bool order_valid = false;
 
     uint32_t* d_error = nullptr;
     uint32_t* d_work = nullptr;
@@ -334,7 +342,42 @@ int ensure_target(orn_context* ctx) {
     ORN_CUDA(ctx, cudaMemsetAsync(ctx->acc, 0, n * sizeof(float4), ctx->stream));
     ORN_CUDA(ctx, cudaMemsetAsync(ctx->fb, 0, n * sizeof(float4), ctx->stream));
     ORN_CUDA(ctx, orn::launch_seed_rng(ctx->rng, (uint32_t)n, ctx->stream));
+    const size_t tiles = orn::order_tiles((uint32_t)n);
+    ORN_CUDA(ctx, cudaMalloc(&ctx->px_cost, n * sizeof(uint32_t)));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->px_order, n * sizeof(uint32_t)));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->tile_buf, 4 * tiles * sizeof(uint32_t)));
+    ORN_CUDA(ctx, orn::order_temp_bytes((uint32_t)n, &ctx->sort_temp_bytes));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->sort_temp, std::max<size_t>(ctx->sort_temp_bytes, 16)));
+    ctx->order_valid = false;
     ctx->target_valid = true;
+    return ORN_OK;
+}
+
+// Points a launch at the pixel order (when one exists and the state asks for
+// it) and at the cost buffer the launch fills.
+void use_pixel_order(orn_context* ctx, RenderLaunch* p) {
+    const bool on = ctx->state.pixel_order == ORN_PIXEL_ORDER_COST;
+    p->order = on && ctx->order_valid ? ctx->px_order : nullptr;
+    p->cost = on ? ctx->px_cost : nullptr;
+}
+
+// After a launch that recorded costs: the order for the next launch.
+int update_pixel_order(orn_context* ctx, const RenderLaunch& p) {
+    if (!p.cost) return ORN_OK;
+    const size_t tiles = orn::order_tiles(p.pixel_count);
+    orn::PixelOrder o;
+    o.cost = ctx->px_cost;
+    o.pixels = p.pixel_count;
+    o.keys = ctx->tile_buf;
+    o.vals = ctx->tile_buf + tiles;
+    o.keys2 = ctx->tile_buf + 2 * tiles;
+    o.vals2 = ctx->tile_buf + 3 * tiles;
+    o.temp = ctx->sort_temp;
+    o.temp_bytes = ctx->sort_temp_bytes;
+    o.order = ctx->px_order;
+    ORN_CUDA(ctx, orn::launch_pixel_order(o, ctx->stream));
+    ctx->launches += 2;   // tile costs and the order (the radix sort between them is CUB's)
+    ctx->order_valid = true;
     return ORN_OK;
 }
 
@@ -352,12 +395,17 @@ void free_cache_buffers(orn_context* ctx) {
 }
 
 void free_target(orn_context* ctx) {
-    if (ctx->acc) cudaFree(ctx->acc);
-    if (ctx->fb) cudaFree(ctx->fb);
-    if (ctx->rng) cudaFree(ctx->rng);
+    void* ptrs[] = {ctx->acc, ctx->fb, ctx->rng, ctx->px_cost, ctx->px_order, ctx->tile_buf, ctx->sort_temp};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
     ctx->acc = nullptr;
     ctx->fb = nullptr;
     ctx->rng = nullptr;
+    ctx->px_cost = nullptr;
+    ctx->px_order = nullptr;
+    ctx->tile_buf = nullptr;
+    ctx->sort_temp = nullptr;
+    ctx->order_valid = false;
     ctx->target_valid = false;
 }
 
@@ -866,7 +914,7 @@ int orn_destroy(orn_context* ctx) {
 int orn_set_state(orn_context* ctx, const orn_state* s) {
     if (!ctx || !s) return ORN_ERR_INVALID_ARGUMENT;
     if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED ||
-        s->triangle_test > ORN_TRIANGLE_WATERTIGHT)
+        s->triangle_test > ORN_TRIANGLE_WATERTIGHT || s->pixel_order > ORN_PIXEL_ORDER_RASTER)
         return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics, kernel or triangle test");
     ctx->state = *s;
     ctx->scene.watertight = s->triangle_test == ORN_TRIANGLE_WATERTIGHT ? 1u : 0u;
@@ -983,9 +1031,12 @@ int orn_render(orn_context* ctx) {
             st = render_wavefront_sweep(ctx, p.cp, n, p.do_post != 0);
             if (st) return st;
         } else {
+            use_pixel_order(ctx, &p);
             ORN_CUDA(ctx, orn::launch_mega(p, (int)ctx->state.semantics, orn::MATH_PORTABLE,
                                            ctx->counters_enabled, render_fast_slabs(ctx), ctx->stream));
             ctx->launches++;
+            st = update_pixel_order(ctx, p);
+            if (st) return st;
         }
         done += n;
     }
@@ -1117,8 +1168,13 @@ int orn_render_f64(orn_context* ctx, uint32_t spp, double* mean_rgba, size_t pix
             uint32_t k = std::min(chunk, spp - done);
             p.cp = make_params(ctx, 1.0f + (float)done);
             p.spp = k;
+            if (ctx->target_valid) use_pixel_order(ctx, &p);
             ORN_CUDA(ctx, orn::launch_mega_f64(p, (int)ctx->state.semantics, fast, ctx->stream));
             ctx->launches++;
+            if (ctx->target_valid) {
+                int ost = update_pixel_order(ctx, p);
+                if (ost) return ost;
+            }
             done += k;
         }
         std::vector<double> host(n * 4);

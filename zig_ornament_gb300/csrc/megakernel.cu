@@ -97,6 +97,7 @@ mega_kernel(RenderLaunch p) {
     int mode = LANE_IDLE;
     bool exhausted = false;          // warp-uniform: the pixel counter ran out
     uint32_t gid = 0, k = 0, bounce = 0;
+    uint32_t steps = 0;              // traversal steps of the current pixel (its cost)
     Rng rng{0};
     Accum<F64> acc;
     acc.load(p, 0, 0.0f);
@@ -145,6 +146,7 @@ mega_kernel(RenderLaunch p) {
         }
         acc.store(p, gid);
         p.rng[gid] = rng.state;
+        if (p.cost) p.cost[gid] = steps;
         if constexpr (!F64 && !CACHE) {
             if (p.do_post) {
                 uint32_t x = gid % W, y = gid / W;
@@ -168,7 +170,8 @@ mega_kernel(RenderLaunch p) {
             if (mode == LANE_IDLE) {
                 uint32_t mine = base + __popc(idle & lanes_below);
                 if (mine < p.pixel_count) {
-                    gid = mine;
+                    gid = p.order ? p.order[mine] : mine;
+                    steps = 0;
                     rng.state = p.rng[gid];
                     acc.load(p, gid, ci0);
                     k = 0;
@@ -188,6 +191,7 @@ mega_kernel(RenderLaunch p) {
         if (mode == LANE_TRAVERSE) {
 #pragma unroll 1
             for (int s = 0; s < kStepsPerIteration; ++s) {
+                ++steps;
                 if (!walker_step<COUNT, kSmemStack, FAST>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon, &h, stack, &vc, &err)) {
                     mode = LANE_SHADE;
                     break;

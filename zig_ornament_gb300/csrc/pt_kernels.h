@@ -100,7 +100,28 @@ struct RenderLaunch {
     double* acc64;             // FP64 accumulation (orn_render_f64 only)
     int shade_threshold;       // ready lanes needed before a warp shades
     CacheLaunch cache;         // cached launches only
+    const uint32_t* order;     // hand-out order of the pixels (null: raster order)
+    uint32_t* cost;            // per-pixel traversal steps of this launch (or null)
 };
+
+// Longest-first pixel order (order.cu): from the per-pixel costs of one
+// launch, the hand-out order of the next (tiles of 32 pixels by decreasing
+// summed cost).  Buffers: keys/vals/keys2/vals2 one entry per tile, `temp`
+// of order_temp_bytes.
+struct PixelOrder {
+    const uint32_t* cost;
+    uint32_t pixels;
+    uint32_t* keys;
+    uint32_t* vals;
+    uint32_t* keys2;
+    uint32_t* vals2;
+    void* temp;
+    size_t temp_bytes;
+    uint32_t* order;
+};
+uint32_t order_tiles(uint32_t pixels);
+cudaError_t order_temp_bytes(uint32_t pixels, size_t* bytes);
+cudaError_t launch_pixel_order(const PixelOrder& o, cudaStream_t s);
 
 #ifndef ORN_SHADE_THRESHOLD
 #define ORN_SHADE_THRESHOLD 8

@@ -295,6 +295,7 @@ class State:
         self.kernel = _lib.KERNEL_MEGA
         self.spp_per_launch = 0
         self.triangle_test = _lib.TRIANGLE_MOLLER_TRUMBORE
+        self.pixel_order = _lib.PIXEL_ORDER_COST
 
     def setFlipY(self, v): self.flip_y = bool(v)
     def getFlipY(self): return self.flip_y
@@ -322,6 +323,7 @@ class State:
         s.kernel = self.kernel
         s.spp_per_launch = self.spp_per_launch
         s.triangle_test = self.triangle_test
+        s.pixel_order = self.pixel_order
         return s
 
 
