@@ -57,6 +57,7 @@ def _run(cmd):
 def build_library(force: bool = False, verbose: bool = False) -> Path:
     """Compiles and links libornament_cuda.so; returns its path."""
     if not force and LIB.exists() and LIB.stat().st_mtime >= _newest_input():
+        build_driver()
         return LIB
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
@@ -78,7 +79,23 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     tmp = LIB.with_suffix(".so.tmp")
     _run([nvcc, "-shared", *ARCH, "-o", str(tmp), *objs, "-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, LIB)
+    build_driver(force=True)
     return LIB
+
+
+DRIVER_SRC = PKG / "driver" / "orn_headless.c"
+DRIVER = PKG / "orn_headless"
+
+
+def build_driver(force: bool = False) -> Path:
+    """The plain-C headless frame loop (driver/orn_headless.c), linked
+    against the in-tree library with an $ORIGIN rpath."""
+    if not force and DRIVER.exists() and DRIVER.stat().st_mtime >= max(
+            DRIVER_SRC.stat().st_mtime, LIB.stat().st_mtime):
+        return DRIVER
+    _run(["gcc", "-std=c11", "-O2", "-Wall", "-Wextra", "-D_POSIX_C_SOURCE=200809L", f"-I{INCLUDE}",
+          str(DRIVER_SRC), "-o", str(DRIVER), f"-L{PKG}", "-lornament_cuda", "-Wl,-rpath,$ORIGIN", "-lm"])
+    return DRIVER
 
 
 if __name__ == "__main__":
