@@ -464,14 +464,16 @@ def relmse_scene(name, w, h):
 
 
 def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=None, warmup=64, methods=None,
-                   ref=None):
+                   ref=None, streams=8, batched_warmup_spp=32):
     """GPU time each renderer needs to bring the relMSE against an FP64
     `ref_spp`-sample oracle (orn_render_f64) down to `target`: plain
     megakernel tracing, the cached renderer without the network (every pixel
     traces its full path with light sampling: unbiased), the cached
     renderer as configured (lr 1e-3, 64 warm-up training frames counted),
     and the cached renderer tuned: on the SAH tree (a non-parity tree, like
-    the cached renderer itself), Adam lr 3e-3, 32 warm-up frames.  Progressive rendering
+    the cached renderer itself), Adam lr 3e-3, 32 warm-up frames; and
+    cached + batched: the tuned renderer with `streams` sample streams per
+    pixel batched into each frame's launch (orn_state.spp_per_launch).  Progressive rendering
     in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
     chunks outside the timed renders; the crossing is interpolated
     log-linearly between the two chunks around it, or extrapolated as
@@ -500,17 +502,23 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         rr.close()
     ref_s = time.time() - t0
     out = {"resolution": f"{w}x{h}", "reference_spp": ref_spp, "reference_seconds": round(ref_s, 1)}
-    for method in (methods or ("plain", "light_sampling", "cached", "cached_tuned")):
+    for method in (methods or ("plain", "light_sampling", "cached", "cached_tuned", "cached_batched")):
         kernel = _lib.KERNEL_MEGA if method == "plain" else _lib.KERNEL_CACHED
-        tuned = method == "cached_tuned"
+        tuned = method in ("cached_tuned", "cached_batched")
         if tuned and bvh_sah is None:
             bvh_sah = ornament.Bvh(scene, row_major_transforms=True, builder="sah")
         r, st = renderer(kernel, bvh_sah if tuned else None)
+        if method == "cached_batched":
+            st.spp_per_launch = streams
         cache = None
         t = 0.0
         if method != "plain":
             if method == "light_sampling":
                 cfg = {"train_shift": 0, "steps_per_frame": 0}
+            elif method == "cached_batched":
+                # the same training per sample as cached_tuned: every stream
+                # trains, so the frame's training steps scale with the streams
+                cfg = {"train_shift": 3, "learning_rate": 3e-3, "steps_per_frame": 4 * streams}
             elif tuned:
                 cfg = {"train_shift": 3, "learning_rate": 3e-3}
             else:
@@ -518,7 +526,11 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             cache = ornament.RadianceCache(seed=1, **cfg)
             r.attach_cache(cache)
         if method.startswith("cached"):
-            st.iterations = 32 if tuned else warmup   # warm-up training, then the accumulation restarts
+            # warm-up training, then the accumulation restarts
+            if method == "cached_batched":
+                st.iterations = max(1, -(-batched_warmup_spp // streams))
+            else:
+                st.iterations = 32 if tuned else warmup
             r.set_state(st.to_struct())
             r.render()
             t += r.last_render_ms() / 1e3
@@ -529,7 +541,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             r.set_state(st.to_struct())
             r.render()
             t += r.last_render_ms() / 1e3
-            n += chunk
+            n += chunk * (streams if method == "cached_batched" else 1)
             e = r.relmse(ref)
             curve.append((t, n, e))
             if e <= target or t >= budget_s:
@@ -550,7 +562,9 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         r.close()
         if cache is not None:
             cache.close()
-    for m in ("cached", "cached_tuned", "light_sampling"):
+    if "cached_batched" in out:
+        out["cached_batched"]["streams"] = streams
+    for m in ("cached", "cached_tuned", "cached_batched", "light_sampling"):
         if m in out and "plain" in out:
             out[f"speedup_{m}_vs_plain"] = round(out["plain"]["seconds"] / out[m]["seconds"], 3)
     out["_ref"] = ref

@@ -176,7 +176,11 @@ typedef struct orn_state {
     float ray_cast_epsilon;   /* default 1e-3 */
     uint32_t semantics;       /* enum orn_semantics, default HIP */
     uint32_t kernel;          /* enum orn_kernel, default MEGA   */
-    uint32_t spp_per_launch;  /* 0 = library chooses             */
+    uint32_t spp_per_launch;  /* MEGA/WAVEFRONT: passes per launch, 0 = library
+                                 chooses.  CACHED: sample streams per pixel in each
+                                 frame's launch (0 = 1, at most 64), each with its
+                                 own RNG state; more than one fills the GPU at low
+                                 resolutions and adds samples atomically */
     uint32_t triangle_test;   /* enum orn_triangle_test, default MOLLER_TRUMBORE */
     uint32_t pixel_order;     /* enum orn_pixel_order, default COST */
 } orn_state;

@@ -227,3 +227,45 @@ def test_light_sampling_is_unbiased():
     r.close()
     cache.close()
     assert e < 5e-3
+
+
+def test_sample_streams():
+    """Several sample streams per pixel in one cached launch
+    (orn_state.spp_per_launch = 4): every pixel gets frames x 4 samples, and
+    without the network (every pixel traces full paths) the image mean still
+    matches a plain FP64 render."""
+    w, h = 160, 96
+    scene = _cache_scene(w, h)
+    r, st = _renderer(scene, w, h, _lib.KERNEL_CACHED)
+    st.spp_per_launch = 4
+    cache = ornament.RadianceCache(seed=1, batch=2048)
+    r.attach_cache(cache)
+    _run_for(r, st, scene, 8)
+    acc = r.accumulation()
+    assert np.isfinite(acc).all()
+    assert np.all(acc[:, 3] == 32)
+    assert cache.stats()["frames"] == 8
+    fb = r.framebuffer()
+    assert np.isfinite(fb).all() and fb[:, :3].max() > 0
+    r.attach_cache(None)
+    r.close()
+    cache.close()
+
+    ref_r, _ = _renderer(scene, w, h, _lib.KERNEL_MEGA)
+    ref = ref_r.render_f64(8192)
+    ref_r.close()
+    r, st = _renderer(scene, w, h, _lib.KERNEL_CACHED)
+    st.spp_per_launch = 4
+    cache = ornament.RadianceCache(seed=1, train_shift=0, steps_per_frame=0)
+    r.attach_cache(cache)
+    _run_for(r, st, scene, 256)
+    acc = r.accumulation().astype(np.float64)
+    assert np.all(acc[:, 3] == 1024)
+    m = acc[:, :3] / acc[:, 3:4]
+    ok = np.isfinite(m).all(axis=1) & np.isfinite(ref[:, :3]).all(axis=1)
+    mean_s, mean_ref = m[ok].mean(axis=0), ref[ok, :3].mean(axis=0)
+    print("image mean: 4 streams", mean_s.round(5), "reference", mean_ref.round(5))
+    assert np.allclose(mean_s, mean_ref, rtol=3e-3)
+    assert r.relmse(ref) < 5e-3
+    r.close()
+    cache.close()

@@ -385,7 +385,10 @@ def test_pixel_order_does_not_change_results(kernel):
             cache = ornament.RadianceCache(seed=1, train_shift=3, steps_per_frame=0)
             r.attach_cache(cache)
         r.set_resolution(96, 54)
-        st = make_state(depth=8, iterations=6, spp_per_launch=2, kernel=kernel)
+        # (for the cached kernel spp_per_launch counts sample streams, whose
+        # atomic accumulation is not bit-reproducible: one stream there)
+        st = make_state(depth=8, iterations=6, spp_per_launch=2 if kernel == _lib.KERNEL_MEGA else 0,
+                        kernel=kernel)
         st.pixel_order = order
         r.set_state(st)
         r.set_camera(scene.camera.to_struct())

@@ -78,7 +78,8 @@ struct orn_context {
     // radiance cache (ORN_KERNEL_CACHED): the attached cache, the query queue
     // (one entry per pixel at most) and the training slots
     orn_cache* cache = nullptr;
-    uint32_t cq_pixels = 0, cq_slots = 0, cq_shift = 0;
+    uint32_t cq_pixels = 0, cq_slots = 0, cq_shift = 0, cq_streams = 0;
+    uint32_t* rng_extra = nullptr;    // RNG states of sample streams 1.. of cached frames
     uint32_t* cq_count = nullptr;
     uint32_t* cq_pixel = nullptr;
     float* cq_in = nullptr;
@@ -382,9 +383,12 @@ int update_pixel_order(orn_context* ctx, const RenderLaunch& p) {
 }
 
 void free_cache_buffers(orn_context* ctx) {
-    void* ptrs[] = {ctx->cq_count, ctx->cq_pixel, ctx->cq_in, ctx->cq_thr, ctx->ct_in, ctx->ct_target};
+    void* ptrs[] = {ctx->cq_count, ctx->cq_pixel, ctx->cq_in, ctx->cq_thr, ctx->ct_in, ctx->ct_target,
+                    ctx->rng_extra};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    ctx->rng_extra = nullptr;
+    ctx->cq_streams = 0;
     ctx->cq_count = nullptr;
     ctx->cq_pixel = nullptr;
     ctx->cq_in = nullptr;
@@ -551,16 +555,33 @@ int render_wavefront_sweep(orn_context* ctx, const orn_constant_params& cp, uint
 
 // Query queue and training slots of the cached renderer, sized for the
 // current resolution and the cache's training fraction.
+// Sample streams per pixel of a cached frame: orn_state.spp_per_launch
+// (0 = 1), at most 64.
+uint32_t cache_streams(const orn_context* ctx) {
+    return std::min<uint32_t>(std::max<uint32_t>(ctx->state.spp_per_launch, 1u), 64u);
+}
+
 int ensure_cache_buffers(orn_context* ctx) {
     const uint32_t n = ctx->width * ctx->height;
     const uint32_t shift = ctx->cache->config.train_shift;
-    if (ctx->cq_count && ctx->cq_pixels == n && ctx->cq_shift == shift) return ORN_OK;
+    const uint32_t streams = cache_streams(ctx);
+    if (ctx->cq_count && ctx->cq_pixels == n && ctx->cq_shift == shift && ctx->cq_streams == streams) return ORN_OK;
+    if ((uint64_t)n * streams >= 0xFFFFFFFFull)
+        return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "pixels x sample streams exceeds 2^32");
     free_cache_buffers(ctx);
-    const uint32_t slots = orn::cache_train_slots(n, shift);
+    const uint32_t slots = orn::cache_train_slots(n, shift) * streams;   // every stream trains
+    const size_t queries = (size_t)n * streams;   // one query per stream and pixel at most
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_count, 4));
-    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_pixel, (size_t)n * 4));
-    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_in, (size_t)n * orn::kCacheInputs * 4));
-    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_thr, (size_t)n * sizeof(float4)));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_pixel, queries * 4));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_in, queries * orn::kCacheInputs * 4));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cq_thr, queries * sizeof(float4)));
+    if (streams > 1) {
+        // stream s of pixel i starts from state s * pixels + i (stream 0 is
+        // the pixel's own state, seeded with i)
+        ORN_CUDA(ctx, cudaMalloc(&ctx->rng_extra, (size_t)(streams - 1) * n * 4));
+        ORN_CUDA(ctx, orn::launch_seed_rng(ctx->rng_extra, (streams - 1) * n, ctx->stream, n));
+    }
+    ctx->cq_streams = streams;
     ORN_CUDA(ctx, cudaMalloc(&ctx->ct_in, (size_t)slots * orn::kCacheInputs * 4));
     ORN_CUDA(ctx, cudaMalloc(&ctx->ct_target, (size_t)slots * 3 * 4));
     // training inputs must stay finite even in slots no path writes
@@ -584,6 +605,11 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     const uint32_t steps = std::min(c->config.steps_per_frame, nb);
     p.do_post = 0;
     p.spp = 1;
+    const uint32_t streams = ctx->cq_streams;
+    p.cache.streams = streams;
+    p.cache.rng_extra = ctx->rng_extra;
+    if (streams > 1 && ci_start <= 1.0f)   // restarted accumulation: the streams add to zero
+        ORN_CUDA(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)n * sizeof(float4), ctx->stream));
     for (int k = 0; k < 3; ++k) {
         p.cache.lo[k] = ctx->scene_lo[k];
         const float ext = ctx->scene_hi[k] - ctx->scene_lo[k];
@@ -596,21 +622,21 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     p.cache.query_thr = ctx->cq_thr;
     p.cache.train_in = ctx->ct_in;
     p.cache.train_target = ctx->ct_target;
-    p.cache.train_slots = ctx->cq_slots;
+    p.cache.train_slots = ctx->cq_slots / streams;
     p.cache.light_count = ctx->light_count;
     p.cache.light_area = ctx->light_area;
     p.cache.lights = ctx->d_lights;
     p.cache.light_cdf = ctx->d_light_cdf;
     p.cache.light_material = ctx->d_light_material;
     for (uint32_t f = 0; f < passes; ++f) {
-        p.cp = make_params(ctx, ci_start + (float)f);
+        p.cp = make_params(ctx, ci_start + (float)(f * streams));
         p.cache.frame = (uint32_t)c->frames;
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->cq_count, 0, 4, ctx->stream));
         // slots no training path writes this frame read as "no target" (NaN)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->ct_target, 0xFF, (size_t)ctx->cq_slots * 12, ctx->stream));
         ORN_CUDA(ctx, orn::launch_mega_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
         ctx->launches++;
-        int st = orn::cache_apply_queries(c, ctx->cq_count, n, ctx->cq_in, ctx->cq_pixel, ctx->cq_thr, ctx->acc,
+        int st = orn::cache_apply_queries(c, ctx->cq_count, n * streams, ctx->cq_in, ctx->cq_pixel, ctx->cq_thr, ctx->acc,
                                           ctx->d_error, ctx->stream);
         if (st) return fail(ctx, st, c->last_error);
         for (uint32_t k = 0; k < steps; ++k) {
@@ -625,7 +651,7 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     }
     if (p.pixel_count) {
         ORN_CUDA(ctx, orn::launch_post(ctx->acc, ctx->fb, ctx->width, ctx->height, ctx->state.flip_y ? 1u : 0u,
-                                       ci_start + (float)(passes - 1), ctx->state.inverted_gamma,
+                                       ci_start + (float)(passes * streams - 1), ctx->state.inverted_gamma,
                                        (int)ctx->state.semantics, orn::MATH_PORTABLE, ctx->stream));
     }
     return ORN_OK;
@@ -989,7 +1015,8 @@ int orn_render(orn_context* ctx) {
     // iterations <= 1 takes the fused path of the reference: one pass.
     const uint32_t passes = std::max<uint32_t>(ctx->state.iterations, 1u);
     const float ci_start = ctx->current_iteration + 1.0f;
-    ctx->current_iteration += (float)passes;
+    // a cached frame takes cache_streams() samples per pixel
+    ctx->current_iteration += (float)passes * (ctx->state.kernel == ORN_KERNEL_CACHED ? cache_streams(ctx) : 1u);
     uint32_t chunk = ctx->state.spp_per_launch;
     if (chunk == 0) chunk = passes <= 64 ? passes : 32;
     RenderLaunch p;

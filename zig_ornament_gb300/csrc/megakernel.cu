@@ -20,6 +20,7 @@ namespace orn {
 
 enum LaneMode { LANE_IDLE = 0, LANE_TRAVERSE = 1, LANE_SHADE = 2, LANE_DONE = 3 };
 
+
 // Solid-angle density of the reference's lambertian scatter direction
 // w = normalize(n + s), s = normalize(in_unit_sphere()) (material.hip.h,
 // random.hip.h), whose polar angle about the world z axis is uniform in
@@ -98,6 +99,9 @@ mega_kernel(RenderLaunch p) {
     bool exhausted = false;          // warp-uniform: the pixel counter ran out
     uint32_t gid = 0, k = 0, bounce = 0;
     uint32_t steps = 0;              // traversal steps of the current pixel (its cost)
+    uint32_t stream = 0;             // cached launches: the sample stream of the current item
+    const uint32_t items = CACHE ? p.pixel_count * p.cache.streams : p.pixel_count;
+    const bool atomic_acc = CACHE && p.cache.streams > 1u;
     Rng rng{0};
     Accum<F64> acc;
     acc.load(p, 0, 0.0f);
@@ -121,6 +125,20 @@ mega_kernel(RenderLaunch p) {
     uint32_t shadow_inv = 0;
     f3 qthr = mk(0.0f, 0.0f, 0.0f);   // a query's throughput x surface colour
 
+    // Adds a finished sample to the pixel: in registers, or atomically when
+    // several streams of a cached launch share the pixel.
+    auto add_sample = [&](f3 c) {
+        if (atomic_acc) {
+            float* a = reinterpret_cast<float*>(p.acc + gid);
+            atomicAdd(a + 0, c.x);
+            atomicAdd(a + 1, c.y);
+            atomicAdd(a + 2, c.z);
+            atomicAdd(a + 3, 1.0f);
+        } else {
+            acc.add(ci0 + (float)k, c);
+        }
+    };
+
     // Starts sample k of the current pixel; returns the lane's next mode.
     // Samples with depth 0 finish immediately (the bounce loop never runs).
     auto start_samples = [&]() -> int {
@@ -141,11 +159,15 @@ mega_kernel(RenderLaunch p) {
                 walker_begin(w, p.scene, ro, rd);
                 return LANE_TRAVERSE;
             }
-            acc.add(ci0 + (float)k, color);
+            add_sample(color);
             ++k;
         }
-        acc.store(p, gid);
-        p.rng[gid] = rng.state;
+        if (CACHE && stream > 0u) {
+            p.cache.rng_extra[(size_t)(stream - 1u) * p.pixel_count + gid] = rng.state;
+        } else {
+            if (!atomic_acc) acc.store(p, gid);
+            p.rng[gid] = rng.state;
+        }
         if (p.cost) p.cost[gid] = steps;
         if constexpr (!F64 && !CACHE) {
             if (p.do_post) {
@@ -166,18 +188,26 @@ mega_kernel(RenderLaunch p) {
             uint32_t base = 0;
             if (lane == leader) base = atomicAdd(p.work_counter, n);
             base = __shfl_sync(kFull, base, leader);
-            if (base + n >= p.pixel_count) exhausted = true;
+            if (base + n >= items) exhausted = true;
             if (mode == LANE_IDLE) {
                 uint32_t mine = base + __popc(idle & lanes_below);
-                if (mine < p.pixel_count) {
-                    gid = p.order ? p.order[mine] : mine;
+                if (mine < items) {
                     steps = 0;
-                    rng.state = p.rng[gid];
-                    acc.load(p, gid, ci0);
                     k = 0;
                     if constexpr (CACHE) {
+                        stream = mine / p.pixel_count;
+                        gid = mine - stream * p.pixel_count;
+                        rng.state = stream > 0u ? p.cache.rng_extra[(size_t)(stream - 1u) * p.pixel_count + gid]
+                                                : p.rng[gid];
+                        if (atomic_acc) acc.load(p, gid, 0.0f);   // zero: the samples are added atomically
+                        else acc.load(p, gid, ci0);
+                        // every stream has its own block of training slots
                         tslot = cache_train_slot(gid, p.cache.frame, p.cache.train_shift);
-                        if (tslot >= p.cache.train_slots) tslot = 0xffffffffu;
+                        tslot = tslot < p.cache.train_slots ? tslot + stream * p.cache.train_slots : 0xffffffffu;
+                    } else {
+                        gid = p.order ? p.order[mine] : mine;
+                        rng.state = p.rng[gid];
+                        acc.load(p, gid, ci0);
                     }
                     mode = start_samples();
                 }
@@ -417,7 +447,7 @@ mega_kernel(RenderLaunch p) {
                             tg[2] = v2 ? L.z : 0.0f;
                             if (v2) c = add(Lpre, mul(pre, L));
                         }
-                        acc.add(ci0 + (float)k, c);
+                        add_sample(c);
                         ++k;
                         mode = start_samples();
                     }
@@ -491,9 +521,9 @@ trace_rays_kernel(SceneDev sc, float t_min, const float* __restrict__ rays, size
 
 // Reseeds every pixel's RNG state with its pixel index
 // (src/hip_backend/buffers.zig:27-31).
-__global__ void seed_rng_kernel(uint32_t* rng, uint32_t n) {
+__global__ void seed_rng_kernel(uint32_t* rng, uint32_t n, uint32_t first) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rng[i] = i;
+    if (i < n) rng[i] = first + i;
 }
 
 // Post-processing alone (post_processing_kernal, pathtracer.hip.cpp:44-56).
@@ -632,8 +662,8 @@ cudaError_t launch_trace_rays(const SceneDev& sc, float t_min, const float* rays
     return cudaGetLastError();
 }
 
-cudaError_t launch_seed_rng(uint32_t* rng, uint32_t n, cudaStream_t s) {
-    seed_rng_kernel<<<(n + 255) / 256, 256, 0, s>>>(rng, n);
+cudaError_t launch_seed_rng(uint32_t* rng, uint32_t n, cudaStream_t s, uint32_t first) {
+    seed_rng_kernel<<<(n + 255) / 256, 256, 0, s>>>(rng, n, first);
     return cudaGetLastError();
 }
 

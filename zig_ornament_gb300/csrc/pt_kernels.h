@@ -61,7 +61,7 @@ struct CacheLaunch {
     float4* query_thr;
     float* train_in;           // [slots][10]
     float* train_target;       // [slots][3]; x = -1 when the path had no cache vertex
-    uint32_t train_slots;
+    uint32_t train_slots;      // per stream
     // next-event estimation: emissive mesh triangles, 4 float4 each (v0, e1,
     // e2 with the emission in .w; the emitter's inverse-transform id in the
     // x bits of the fourth), their cumulative areas, and a flag per material
@@ -71,6 +71,13 @@ struct CacheLaunch {
     const float4* lights;
     const float* light_cdf;
     const uint32_t* light_material;
+    // sample streams per pixel in this launch: stream 0 continues the pixel's
+    // own RNG state, stream s > 0 its own state in rng_extra[(s-1) * pixels +
+    // pixel]; with more than one the samples are added to the accumulation
+    // atomically (the host zeroes it first).  Stream s uses training slots
+    // [s * train_slots, (s + 1) * train_slots).
+    uint32_t streams;
+    uint32_t* rng_extra;
 };
 
 // Training slot of pixel `gid` in frame `frame`, or 0xffffffff when the
@@ -185,7 +192,7 @@ cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, i
 cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, bool fast, cudaStream_t s);
 cudaError_t launch_trace_rays(const SceneDev& sc, float t_min, const float* rays, size_t count,
                               orn_hit* hits, uint32_t* visits, uint32_t* error, cudaStream_t s);
-cudaError_t launch_seed_rng(uint32_t* rng, uint32_t n, cudaStream_t s);
+cudaError_t launch_seed_rng(uint32_t* rng, uint32_t n, cudaStream_t s, uint32_t first = 0);   // rng[i] = first + i
 cudaError_t launch_post(const float4* acc, float4* fb, uint32_t W, uint32_t H, uint32_t flip_y,
                         float ci, float inv_gamma, int semantics, int math, cudaStream_t s);
 

@@ -214,13 +214,15 @@ rc_forward(RcForward p) {
             } else if (valid) {
                 if (!TRAIN) {
                     if (p.pixel) {
+                        // atomic: several sample streams of a pixel may query in
+                        // one frame (one add each, so one query gives the same bits
+                        // as a plain read-modify-write)
                         const uint32_t px = p.pixel[row];
                         const float4 th = p.throughput[row];
-                        float4 a = p.acc[px];
-                        a.x += th.x * fminf(fmaxf(v[0], 0.0f), 1.0e4f);
-                        a.y += th.y * fminf(fmaxf(v[1], 0.0f), 1.0e4f);
-                        a.z += th.z * fminf(fmaxf(v[2], 0.0f), 1.0e4f);
-                        p.acc[px] = a;
+                        float* a = reinterpret_cast<float*>(p.acc + px);
+                        atomicAdd(a + 0, th.x * fminf(fmaxf(v[0], 0.0f), 1.0e4f));
+                        atomicAdd(a + 1, th.y * fminf(fmaxf(v[1], 0.0f), 1.0e4f));
+                        atomicAdd(a + 2, th.z * fminf(fmaxf(v[2], 0.0f), 1.0e4f));
                     }
                     if (p.outputs)
                         for (int c = 0; c < kOutputs; ++c) p.outputs[(size_t)row * kOutputs + c] = v[c];
