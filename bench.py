@@ -464,7 +464,7 @@ def relmse_scene(name, w, h):
 
 
 def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=None, warmup=64, methods=None,
-                   ref=None, streams=8, batched_warmup_spp=32):
+                   ref=None, streams=8, batched_warmup_spp=32, batched_sobol=True, batched_cfg=None):
     """GPU time each renderer needs to bring the relMSE against an FP64
     `ref_spp`-sample oracle (orn_render_f64) down to `target`: plain
     megakernel tracing, the cached renderer without the network (every pixel
@@ -472,8 +472,10 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
     renderer as configured (lr 1e-3, 64 warm-up training frames counted),
     and the cached renderer tuned: on the SAH tree (a non-parity tree, like
     the cached renderer itself), Adam lr 3e-3, 32 warm-up frames; and
-    cached + batched: the tuned renderer with `streams` sample streams per
-    pixel batched into each frame's launch (orn_state.spp_per_launch).  Progressive rendering
+    cached + batched: on the SAH tree, `streams` sample streams per pixel
+    batched into each frame's launch (orn_state.spp_per_launch), the Sobol
+    sampler, a quarter of the pixels training at lr 5e-3, a 32-sample
+    warm-up.  Progressive rendering
     in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
     chunks outside the timed renders; the crossing is interpolated
     log-linearly between the two chunks around it, or extrapolated as
@@ -510,15 +512,18 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         r, st = renderer(kernel, bvh_sah if tuned else None)
         if method == "cached_batched":
             st.spp_per_launch = streams
+            st.sampler = _lib.SAMPLER_SOBOL if batched_sobol else _lib.SAMPLER_PCG
         cache = None
         t = 0.0
         if method != "plain":
             if method == "light_sampling":
                 cfg = {"train_shift": 0, "steps_per_frame": 0}
             elif method == "cached_batched":
-                # the same training per sample as cached_tuned: every stream
-                # trains, so the frame's training steps scale with the streams
-                cfg = {"train_shift": 3, "learning_rate": 3e-3, "steps_per_frame": 4 * streams}
+                # every stream trains on its own slots; a quarter of the pixels
+                # train (the open scene has little training data per pixel:
+                # most primary rays reach the sky), one pass over the frame's
+                # training data (steps capped by the slots)
+                cfg = batched_cfg or {"train_shift": 2, "learning_rate": 5e-3, "steps_per_frame": 64}
             elif tuned:
                 cfg = {"train_shift": 3, "learning_rate": 3e-3}
             else:

@@ -183,7 +183,17 @@ typedef struct orn_state {
                                  resolutions and adds samples atomically */
     uint32_t triangle_test;   /* enum orn_triangle_test, default MOLLER_TRUMBORE */
     uint32_t pixel_order;     /* enum orn_pixel_order, default COST */
+    uint32_t sampler;         /* enum orn_sampler, default PCG */
 } orn_state;
+
+/* Random numbers of the cached kernel (no counterpart in the reference).
+ * PCG: the reference's per-pixel stream (random.hip.h:14-30), as every other
+ * kernel always uses.  SOBOL: each pixel's jitter, lens, first-bounce
+ * direction and first light sample come from 2-D Owen-scrambled Sobol
+ * points (Burley 2020), stratified over the pixel's samples since the last
+ * camera change; the rest from the stream.  Unbiased; fewer samples to a
+ * given error where pixel footprint and first-bounce visibility dominate. */
+enum orn_sampler { ORN_SAMPLER_PCG = 0, ORN_SAMPLER_SOBOL = 1 };
 
 /* Order in which a plain megakernel launch (ORN_KERNEL_MEGA, and
  * orn_render_f64) hands pixels to lanes (no counterpart in the reference,

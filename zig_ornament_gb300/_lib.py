@@ -36,6 +36,7 @@ BATCH_MAX = 64
 BVH_REFERENCE, BVH_SAH, BVH_LBVH = 0, 1, 2
 TRIANGLE_MOLLER_TRUMBORE, TRIANGLE_WATERTIGHT = 0, 1
 PIXEL_ORDER_COST, PIXEL_ORDER_RASTER = 0, 1
+SAMPLER_PCG, SAMPLER_SOBOL = 0, 1
 COUNTER_NAMES = ["samples", "rays", "visits", "internal", "sphere_leaf", "mesh_entry", "triangle",
                  "sphere_hits", "mesh_hits", "textured_hits"]
 
@@ -94,7 +95,8 @@ class State(C.Structure):
     _fields_ = [("depth", C.c_uint32), ("flip_y", C.c_uint32), ("inverted_gamma", C.c_float),
                 ("iterations", C.c_uint32), ("ray_cast_epsilon", C.c_float),
                 ("semantics", C.c_uint32), ("kernel", C.c_uint32), ("spp_per_launch", C.c_uint32),
-                ("triangle_test", C.c_uint32), ("pixel_order", C.c_uint32)]
+                ("triangle_test", C.c_uint32), ("pixel_order", C.c_uint32),
+                ("sampler", C.c_uint32)]
 
 
 class Ray(C.Structure):

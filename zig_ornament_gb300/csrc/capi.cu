@@ -608,6 +608,7 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     const uint32_t streams = ctx->cq_streams;
     p.cache.streams = streams;
     p.cache.rng_extra = ctx->rng_extra;
+    p.cache.sobol = ctx->state.sampler == ORN_SAMPLER_SOBOL ? 1u : 0u;
     if (streams > 1 && ci_start <= 1.0f)   // restarted accumulation: the streams add to zero
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->acc, 0, (size_t)n * sizeof(float4), ctx->stream));
     for (int k = 0; k < 3; ++k) {
@@ -940,7 +941,8 @@ int orn_destroy(orn_context* ctx) {
 int orn_set_state(orn_context* ctx, const orn_state* s) {
     if (!ctx || !s) return ORN_ERR_INVALID_ARGUMENT;
     if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED ||
-        s->triangle_test > ORN_TRIANGLE_WATERTIGHT || s->pixel_order > ORN_PIXEL_ORDER_RASTER)
+        s->triangle_test > ORN_TRIANGLE_WATERTIGHT || s->pixel_order > ORN_PIXEL_ORDER_RASTER ||
+        s->sampler > ORN_SAMPLER_SOBOL)
         return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics, kernel or triangle test");
     ctx->state = *s;
     ctx->scene.watertight = s->triangle_test == ORN_TRIANGLE_WATERTIGHT ? 1u : 0u;

@@ -15,6 +15,7 @@
 #include "pt_kernels.h"
 #include "pt_device.cuh"
 #include "pt_machine.cuh"
+#include "qmc.cuh"
 
 namespace orn {
 
@@ -100,6 +101,7 @@ mega_kernel(RenderLaunch p) {
     uint32_t gid = 0, k = 0, bounce = 0;
     uint32_t steps = 0;              // traversal steps of the current pixel (its cost)
     uint32_t stream = 0;             // cached launches: the sample stream of the current item
+    uint32_t qseed = 0, qidx = 0;    // Sobol sampler: the pixel's seed and the sample's index
     const uint32_t items = CACHE ? p.pixel_count * p.cache.streams : p.pixel_count;
     const bool atomic_acc = CACHE && p.cache.streams > 1u;
     Rng rng{0};
@@ -143,7 +145,17 @@ mega_kernel(RenderLaunch p) {
     // Samples with depth 0 finish immediately (the bounce loop never runs).
     auto start_samples = [&]() -> int {
         while (k < p.spp) {
-            camera_ray<MATH>(p.cp, gid % W, gid / W, rng, &ro, &rd);
+            if (CACHE && p.cache.sobol) {
+                // sample index since the last camera change (one pass per launch)
+                qseed = qmc_hash(gid + 1u);
+                qidx = (uint32_t)ci0 - 1u + stream + k;
+                float ju, jv, l0, l1;
+                qmc_point(qseed, QMC_PIXEL, qidx, &ju, &jv);
+                qmc_point(qseed, QMC_LENS, qidx, &l0, &l1);
+                camera_ray_from<MATH>(p.cp, gid % W, gid / W, ju, jv, l0, l1, &ro, &rd);
+            } else {
+                camera_ray<MATH>(p.cp, gid % W, gid / W, rng, &ro, &rd);
+            }
             color = mk(1.0f, 1.0f, 1.0f);
             bounce = 0;
             if (CACHE) {
@@ -331,7 +343,13 @@ mega_kernel(RenderLaunch p) {
                             float ldist = 0.0f;
                             if (nee) {
                                 const float target = rng.f() * p.cache.light_area;
-                                const float u1 = rng.f(), u2 = rng.f();
+                                float u1, u2;
+                                if (p.cache.sobol && bounce == 0u) {
+                                    qmc_point(qseed, QMC_LIGHT, qidx, &u1, &u2);
+                                } else {
+                                    u1 = rng.f();
+                                    u2 = rng.f();
+                                }
                                 uint32_t lo = 0, hi = p.cache.light_count - 1u;
                                 while (lo < hi) {
                                     const uint32_t mid = (lo + hi) >> 1;
@@ -385,7 +403,11 @@ mega_kernel(RenderLaunch p) {
                                     v2 = true;
                                     shadow_pre = shadow_ray;
                                 }
-                                const bool cont = shade_geom<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, g, &ro, &rd, &color, &scn);
+                                const bool preset = p.cache.sobol && bounce == 0u;
+                                float pt = 0.0f, pp = 0.0f;
+                                if (preset) qmc_point(qseed, QMC_BOUNCE, qidx, &pt, &pp);
+                                const bool cont = shade_geom<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, g, &ro, &rd, &color,
+                                                                               &scn, preset, pt, pp);
                                 nee_prev = nee;
                                 nprev = g.normal;
                                 if (!cont) {

@@ -451,6 +451,28 @@ __device__ __forceinline__ void camera_ray(const orn_constant_params& cp, uint32
     *rd = sub(sub(add(add(llc, scale(u, hor)), scale(v, ver)), origin), offset);
 }
 
+// The same camera ray from given uniforms (jitter ju, jv; lens l0, l1) —
+// the cached renderer's Sobol sampler.
+template <int MATH>
+__device__ __forceinline__ void camera_ray_from(const orn_constant_params& cp, uint32_t px, uint32_t py, float ju,
+                                                float jv, float l0, float l1, f3* ro, f3* rd) {
+    float u = ((float)px + ju) / (float)(cp.width - 1);
+    float v = ((float)py + jv) / (float)(cp.height - 1);
+    const orn_camera& cam = cp.camera;
+    const float r = sqrtf(l0);
+    float sa, ca;
+    DevMath<MATH>::sincos(2.0f * 3.14159265358979f * l1, &sa, &ca);
+    f3 rdv = scale(cam.lens_radius, mk(r * ca, r * sa, 0.0f));
+    f3 cu = mk(cam.u[0], cam.u[1], cam.u[2]), cv = mk(cam.v[0], cam.v[1], cam.v[2]);
+    f3 origin = mk(cam.origin[0], cam.origin[1], cam.origin[2]);
+    f3 offset = add(scale(rdv.x, cu), scale(rdv.y, cv));
+    f3 llc = mk(cam.lower_left_corner[0], cam.lower_left_corner[1], cam.lower_left_corner[2]);
+    f3 hor = mk(cam.horizontal[0], cam.horizontal[1], cam.horizontal[2]);
+    f3 ver = mk(cam.vertical[0], cam.vertical[1], cam.vertical[2]);
+    *ro = add(origin, offset);
+    *rd = sub(sub(add(add(llc, scale(u, hor)), scale(v, ver)), origin), offset);
+}
+
 // Miss: sky gradient (pathtracer.hip.cpp:87-93).
 __device__ __forceinline__ f3 sky_color(f3 color, f3 rd) {
     f3 ud = normalize(rd);
@@ -514,10 +536,14 @@ __device__ __forceinline__ HitGeom hit_geometry(const SceneDev& sc, const HitRec
 // Hit shading and material (pathtracer.hip.cpp:95-145, material.hip.h):
 // returns true when the path continues with the scattered ray in (ro, rd),
 // false when it ends (emission or absorption) with `color` final.
+// `preset` (the cached renderer's Sobol sampler): a lambertian scatter takes
+// the polar and azimuthal uniforms of its in_unit_sphere direction from
+// (pu_theta, pu_phi) instead of the stream (the radius is normalised away).
 template <int SEM, int MATH, bool COUNT>
 __device__ __forceinline__ bool shade_geom(const SceneDev& sc, const orn_constant_params& cp, Rng& rng,
                                            const HitRec& h, const HitGeom& g, f3* ro_io, f3* rd_io,
-                                           f3* color_io, SampleCount* scn) {
+                                           f3* color_io, SampleCount* scn, bool preset = false,
+                                           float pu_theta = 0.0f, float pu_phi = 0.0f) {
     typedef DevMath<MATH> M;
     const f3 rd = *rd_io;
     f3 color = *color_io;
@@ -531,7 +557,16 @@ __device__ __forceinline__ bool shade_geom(const SceneDev& sc, const orn_constan
     bool use_tex = SEM == SEM_WGSL ? (tex_id < cp.textures_count && tex_id < sc.textures_len)
                                    : tex_id < sc.textures_len;
     if (mtype == ORN_LAMBERTIAN) {
-        f3 dir = add(normal, normalize(rng.in_unit_sphere<MATH>()));
+        f3 s;
+        if (preset) {
+            float st, ct, sp, cph;
+            DevMath<MATH>::sincos(3.14159265358979f * pu_theta, &st, &ct);
+            DevMath<MATH>::sincos(2.0f * 3.14159265358979f * pu_phi, &sp, &cph);
+            s = mk(st * cph, st * sp, ct);
+        } else {
+            s = rng.in_unit_sphere<MATH>();
+        }
+        f3 dir = add(normal, normalize(s));
         if (fabsf(dir.x) < 1e-8f && fabsf(dir.y) < 1e-8f && fabsf(dir.z) < 1e-8f) dir = normal;
         f3 att = use_tex ? tex_sample(sc.textures[tex_id], hu, hv, SEM == SEM_WGSL) : mk(ma.x, ma.y, ma.z);
         if (COUNT && use_tex) scn->textured++;

@@ -78,6 +78,7 @@ struct CacheLaunch {
     // [s * train_slots, (s + 1) * train_slots).
     uint32_t streams;
     uint32_t* rng_extra;
+    uint32_t sobol;            // ORN_SAMPLER_SOBOL: pixel, lens, first bounce and light from qmc.cuh
 };
 
 // Training slot of pixel `gid` in frame `frame`, or 0xffffffff when the

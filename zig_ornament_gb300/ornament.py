@@ -296,6 +296,7 @@ class State:
         self.spp_per_launch = 0
         self.triangle_test = _lib.TRIANGLE_MOLLER_TRUMBORE
         self.pixel_order = _lib.PIXEL_ORDER_COST
+        self.sampler = _lib.SAMPLER_PCG
 
     def setFlipY(self, v): self.flip_y = bool(v)
     def getFlipY(self): return self.flip_y
@@ -324,6 +325,7 @@ class State:
         s.spp_per_launch = self.spp_per_launch
         s.triangle_test = self.triangle_test
         s.pixel_order = self.pixel_order
+        s.sampler = self.sampler
         return s
 
 
