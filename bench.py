@@ -474,7 +474,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
     the cached renderer itself), Adam lr 3e-3, 32 warm-up frames; and
     cached + batched: on the SAH tree, `streams` sample streams per pixel
     batched into each frame's launch (orn_state.spp_per_launch), the Sobol
-    sampler, a quarter of the pixels training at lr 5e-3, a 32-sample
+    sampler, training slots for 1/8 of the samples at lr 5e-3, a 32-sample
     warm-up.  Progressive rendering
     in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
     chunks outside the timed renders; the crossing is interpolated
@@ -519,11 +519,10 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             if method == "light_sampling":
                 cfg = {"train_shift": 0, "steps_per_frame": 0}
             elif method == "cached_batched":
-                # every stream trains on its own slots; a quarter of the pixels
-                # train (the open scene has little training data per pixel:
-                # most primary rays reach the sky), one pass over the frame's
-                # training data (steps capped by the slots)
-                cfg = batched_cfg or {"train_shift": 2, "learning_rate": 5e-3, "steps_per_frame": 64}
+                # training slots for 1/8 of the samples, filled at cache
+                # vertices; one pass over the frame's training data (steps
+                # capped by the slots)
+                cfg = batched_cfg or {"train_shift": 3, "learning_rate": 5e-3, "steps_per_frame": 64}
             elif tuned:
                 cfg = {"train_shift": 3, "learning_rate": 3e-3}
             else:

@@ -416,9 +416,15 @@ typedef struct orn_cache orn_cache;
 
 typedef struct orn_cache_config {
     uint32_t batch;            /* samples per training step, multiple of 128 (default 16384) */
-    uint32_t steps_per_frame;  /* training steps after each cached frame (default 4)          */
-    uint32_t train_shift;      /* one 32-pixel group in 2^train_shift traces full training
-                                  paths each frame (default 4: 1/16 of the pixels)            */
+    uint32_t steps_per_frame;  /* training steps after each cached frame, at most 64 and at
+                                  most the batches the frame's slots fill (default 4)         */
+    uint32_t train_shift;      /* training samples per frame: pixels / 2^train_shift per
+                                  sample stream (default 4).  Paths become training paths
+                                  at their cache vertex, with the probability that fills
+                                  those slots given the previous frame's vertex count; a
+                                  training path runs to its end, the others stop at the
+                                  vertex and query the cache.  0: every path trains (no
+                                  queries: light sampling alone, unbiased)                    */
     float learning_rate;       /* Adam (default 1e-3) */
     float beta1;               /* default 0.9   */
     float beta2;               /* default 0.99  */

@@ -81,6 +81,8 @@ struct orn_context {
     uint32_t cq_pixels = 0, cq_slots = 0, cq_shift = 0, cq_streams = 0;
     uint32_t* rng_extra = nullptr;    // RNG states of sample streams 1.. of cached frames
     uint32_t* cq_count = nullptr;
+    uint32_t* cv_counters = nullptr;  // [training slots taken, cache vertices (two frames, alternating)]
+    uint32_t cv_flip = 0;
     uint32_t* cq_pixel = nullptr;
     float* cq_in = nullptr;
     float4* cq_thr = nullptr;
@@ -384,10 +386,11 @@ int update_pixel_order(orn_context* ctx, const RenderLaunch& p) {
 
 void free_cache_buffers(orn_context* ctx) {
     void* ptrs[] = {ctx->cq_count, ctx->cq_pixel, ctx->cq_in, ctx->cq_thr, ctx->ct_in, ctx->ct_target,
-                    ctx->rng_extra};
+                    ctx->rng_extra, ctx->cv_counters};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     ctx->rng_extra = nullptr;
+    ctx->cv_counters = nullptr;
     ctx->cq_streams = 0;
     ctx->cq_count = nullptr;
     ctx->cq_pixel = nullptr;
@@ -572,6 +575,8 @@ int ensure_cache_buffers(orn_context* ctx) {
     const uint32_t slots = orn::cache_train_slots(n, shift) * streams;   // every stream trains
     const size_t queries = (size_t)n * streams;   // one query per stream and pixel at most
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_count, 4));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cv_counters, 3 * sizeof(uint32_t)));
+    ORN_CUDA(ctx, cudaMemsetAsync(ctx->cv_counters, 0, 3 * sizeof(uint32_t), ctx->stream));
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_pixel, queries * 4));
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_in, queries * orn::kCacheInputs * 4));
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_thr, queries * sizeof(float4)));
@@ -616,14 +621,14 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
         const float ext = ctx->scene_hi[k] - ctx->scene_lo[k];
         p.cache.inv_extent[k] = ext > 0.0f ? 1.0f / ext : 0.0f;
     }
-    p.cache.train_shift = ctx->cq_shift;
     p.cache.query_count = ctx->cq_count;
     p.cache.query_pixel = ctx->cq_pixel;
     p.cache.query_in = ctx->cq_in;
     p.cache.query_thr = ctx->cq_thr;
     p.cache.train_in = ctx->ct_in;
     p.cache.train_target = ctx->ct_target;
-    p.cache.train_slots = ctx->cq_slots / streams;
+    p.cache.train_slots = ctx->cq_slots;
+    p.cache.train_count = ctx->cv_counters;
     p.cache.light_count = ctx->light_count;
     p.cache.light_area = ctx->light_area;
     p.cache.lights = ctx->d_lights;
@@ -631,7 +636,13 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     p.cache.light_material = ctx->d_light_material;
     for (uint32_t f = 0; f < passes; ++f) {
         p.cp = make_params(ctx, ci_start + (float)(f * streams));
-        p.cache.frame = (uint32_t)c->frames;
+        // this frame counts cache vertices into one counter and reads the
+        // other (the previous frame's)
+        p.cache.vertices = ctx->cv_counters + 1 + ctx->cv_flip;
+        p.cache.vertices_prev = ctx->cv_counters + 2 - ctx->cv_flip;
+        ctx->cv_flip ^= 1u;
+        ORN_CUDA(ctx, cudaMemsetAsync(ctx->cv_counters, 0, 4, ctx->stream));
+        ORN_CUDA(ctx, cudaMemsetAsync(p.cache.vertices, 0, 4, ctx->stream));
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->cq_count, 0, 4, ctx->stream));
         // slots no training path writes this frame read as "no target" (NaN)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->ct_target, 0xFF, (size_t)ctx->cq_slots * 12, ctx->stream));

@@ -104,6 +104,12 @@ mega_kernel(RenderLaunch p) {
     uint32_t qseed = 0, qidx = 0;    // Sobol sampler: the pixel's seed and the sample's index
     const uint32_t items = CACHE ? p.pixel_count * p.cache.streams : p.pixel_count;
     const bool atomic_acc = CACHE && p.cache.streams > 1u;
+    float p_train = 1.0f;            // cached launches: the chance that a cache vertex trains
+    if constexpr (CACHE) {
+        const uint32_t prev = *p.cache.vertices_prev;
+        if (prev > p.cache.train_slots) p_train = (float)p.cache.train_slots / (float)prev;
+    }
+    bool vertex = false;             // cached launches: this shading step reached a cache vertex
     Rng rng{0};
     Accum<F64> acc;
     acc.load(p, 0, 0.0f);
@@ -213,9 +219,7 @@ mega_kernel(RenderLaunch p) {
                                                 : p.rng[gid];
                         if (atomic_acc) acc.load(p, gid, 0.0f);   // zero: the samples are added atomically
                         else acc.load(p, gid, ci0);
-                        // every stream has its own block of training slots
-                        tslot = cache_train_slot(gid, p.cache.frame, p.cache.train_shift);
-                        tslot = tslot < p.cache.train_slots ? tslot + stream * p.cache.train_slots : 0xffffffffu;
+                        tslot = 0xffffffffu;   // decided at the cache vertex
                     } else {
                         gid = p.order ? p.order[mine] : mine;
                         rng.state = p.rng[gid];
@@ -247,6 +251,7 @@ mega_kernel(RenderLaunch p) {
             if (mode == LANE_SHADE) {
                 if constexpr (CACHE) {
                     bool end = false, query = false;
+                    vertex = false;
                     float qin[kCacheInputs];
                     if (shadow) {
                         // the shadow ray of a light sample finished: add the sample
@@ -326,6 +331,11 @@ mega_kernel(RenderLaunch p) {
                                 for (int j = 0; j < kCacheInputs; ++j) qin[j] = fminf(fmaxf(q[j], 0.0f), 1.0f);
                                 const f3 a = surface_att();
                                 aclamp = mk(fmaxf(a.x, 1e-3f), fmaxf(a.y, 1e-3f), fmaxf(a.z, 1e-3f));
+                                vertex = true;
+                                if (p_train >= 1.0f || rng.f() < p_train) {
+                                    const uint32_t slot = atomicAdd(p.cache.train_count, 1u);
+                                    if (slot < p.cache.train_slots) tslot = slot;
+                                }
                                 if (tslot == 0xffffffffu) {
                                     query = true;
                                     qthr = mul(color, aclamp);
@@ -444,6 +454,9 @@ mega_kernel(RenderLaunch p) {
                             }
                         }
                     }
+                    // count this warp's cache vertices (one atomic)
+                    const unsigned vm = __ballot_sync(ready, vertex);
+                    if (vm != 0u && lane == __ffs(vm) - 1u) atomicAdd(p.cache.vertices, (unsigned)__popc(vm));
                     // append this warp's queries to the queue (one atomic)
                     const unsigned qm = __ballot_sync(ready, query);
                     if (qm != 0u) {

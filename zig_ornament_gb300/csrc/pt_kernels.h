@@ -51,8 +51,6 @@ constexpr int kCacheInputs = 10;   // position 3, direction 3, normal 3, roughne
 constexpr float kCacheMinFuzz = 0.25f;   // metals below this fuzz are not cache vertices
 
 struct CacheLaunch {
-    uint32_t frame;
-    uint32_t train_shift;
     float lo[3];               // scene bounds: position inputs are (p - lo) * inv_extent
     float inv_extent[3];
     uint32_t* query_count;     // zeroed before the launch
@@ -61,7 +59,14 @@ struct CacheLaunch {
     float4* query_thr;
     float* train_in;           // [slots][10]
     float* train_target;       // [slots][3]; x = -1 when the path had no cache vertex
-    uint32_t train_slots;      // per stream
+    uint32_t train_slots;      // capacity (all streams)
+    // training paths are chosen at the cache vertex: a path that reaches one
+    // trains with probability min(1, train_slots / *vertices_prev) (the
+    // previous frame's count of cache vertices) and takes the next slot from
+    // *train_count while there is one; *vertices counts this frame's vertices
+    uint32_t* train_count;     // zeroed before the launch
+    uint32_t* vertices;        // zeroed before the launch
+    const uint32_t* vertices_prev;
     // next-event estimation: emissive mesh triangles, 4 float4 each (v0, e1,
     // e2 with the emission in .w; the emitter's inverse-transform id in the
     // x bits of the fourth), their cumulative areas, and a flag per material
@@ -74,20 +79,14 @@ struct CacheLaunch {
     // sample streams per pixel in this launch: stream 0 continues the pixel's
     // own RNG state, stream s > 0 its own state in rng_extra[(s-1) * pixels +
     // pixel]; with more than one the samples are added to the accumulation
-    // atomically (the host zeroes it first).  Stream s uses training slots
-    // [s * train_slots, (s + 1) * train_slots).
+    // atomically (the host zeroes it first).
     uint32_t streams;
     uint32_t* rng_extra;
     uint32_t sobol;            // ORN_SAMPLER_SOBOL: pixel, lens, first bounce and light from qmc.cuh
 };
 
-// Training slot of pixel `gid` in frame `frame`, or 0xffffffff when the
-// pixel traces a regular (cache-terminated) path.
-__host__ __device__ __forceinline__ uint32_t cache_train_slot(uint32_t gid, uint32_t frame, uint32_t shift) {
-    const uint32_t group = gid >> 5, period = 1u << shift;
-    if (((group + frame) & (period - 1u)) != 0u) return 0xffffffffu;
-    return (group >> shift) * 32u + (gid & 31u);
-}
+// Training samples a cached frame collects per sample stream: one per
+// 2^shift pixels, in whole groups of 32.
 __host__ __device__ __forceinline__ uint32_t cache_train_slots(uint32_t pixels, uint32_t shift) {
     return ((pixels + (32u << shift) - 1u) >> (5 + shift)) * 32u;
 }
