@@ -81,7 +81,7 @@ struct orn_context {
     uint32_t cq_pixels = 0, cq_slots = 0, cq_shift = 0, cq_streams = 0;
     uint32_t* rng_extra = nullptr;    // RNG states of sample streams 1.. of cached frames
     uint32_t* cq_count = nullptr;
-    uint32_t* cv_counters = nullptr;  // [training slots taken, cache vertices (two frames, alternating)]
+    uint32_t* cv_counters = nullptr;  // [32 training-slot shards, cache vertices (two frames, alternating)]
     uint32_t cv_flip = 0;
     uint32_t* cq_pixel = nullptr;
     float* cq_in = nullptr;
@@ -575,8 +575,8 @@ int ensure_cache_buffers(orn_context* ctx) {
     const uint32_t slots = orn::cache_train_slots(n, shift) * streams;   // every stream trains
     const size_t queries = (size_t)n * streams;   // one query per stream and pixel at most
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_count, 4));
-    ORN_CUDA(ctx, cudaMalloc(&ctx->cv_counters, 3 * sizeof(uint32_t)));
-    ORN_CUDA(ctx, cudaMemsetAsync(ctx->cv_counters, 0, 3 * sizeof(uint32_t), ctx->stream));
+    ORN_CUDA(ctx, cudaMalloc(&ctx->cv_counters, 34 * sizeof(uint32_t)));
+    ORN_CUDA(ctx, cudaMemsetAsync(ctx->cv_counters, 0, 34 * sizeof(uint32_t), ctx->stream));
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_pixel, queries * 4));
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_in, queries * orn::kCacheInputs * 4));
     ORN_CUDA(ctx, cudaMalloc(&ctx->cq_thr, queries * sizeof(float4)));
@@ -636,12 +636,13 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     p.cache.light_material = ctx->d_light_material;
     for (uint32_t f = 0; f < passes; ++f) {
         p.cp = make_params(ctx, ci_start + (float)(f * streams));
+        p.cache.frame = (uint32_t)c->frames;
         // this frame counts cache vertices into one counter and reads the
         // other (the previous frame's)
-        p.cache.vertices = ctx->cv_counters + 1 + ctx->cv_flip;
-        p.cache.vertices_prev = ctx->cv_counters + 2 - ctx->cv_flip;
+        p.cache.vertices = ctx->cv_counters + 32 + ctx->cv_flip;
+        p.cache.vertices_prev = ctx->cv_counters + 33 - ctx->cv_flip;
         ctx->cv_flip ^= 1u;
-        ORN_CUDA(ctx, cudaMemsetAsync(ctx->cv_counters, 0, 4, ctx->stream));
+        ORN_CUDA(ctx, cudaMemsetAsync(ctx->cv_counters, 0, 32 * sizeof(uint32_t), ctx->stream));
         ORN_CUDA(ctx, cudaMemsetAsync(p.cache.vertices, 0, 4, ctx->stream));
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->cq_count, 0, 4, ctx->stream));
         // slots no training path writes this frame read as "no target" (NaN)

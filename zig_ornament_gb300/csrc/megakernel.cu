@@ -83,7 +83,7 @@ template <> struct Accum<true> {
 // first rough surface from the second vertex on) and leaves a query there; a
 // training pixel's path runs to the end and records the network inputs at
 // the cache vertex and the radiance that left it.
-template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false>
+template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false, bool SOBOL = false>
 __global__ void __launch_bounds__(kMegaBlock, CACHE ? 4 : kMegaMinBlocks)
 mega_kernel(RenderLaunch p) {
     __shared__ uint32_t sstack[kSmemStack * kMegaBlock];
@@ -101,14 +101,8 @@ mega_kernel(RenderLaunch p) {
     uint32_t gid = 0, k = 0, bounce = 0;
     uint32_t steps = 0;              // traversal steps of the current pixel (its cost)
     uint32_t stream = 0;             // cached launches: the sample stream of the current item
-    uint32_t qseed = 0, qidx = 0;    // Sobol sampler: the pixel's seed and the sample's index
     const uint32_t items = CACHE ? p.pixel_count * p.cache.streams : p.pixel_count;
     const bool atomic_acc = CACHE && p.cache.streams > 1u;
-    float p_train = 1.0f;            // cached launches: the chance that a cache vertex trains
-    if constexpr (CACHE) {
-        const uint32_t prev = *p.cache.vertices_prev;
-        if (prev > p.cache.train_slots) p_train = (float)p.cache.train_slots / (float)prev;
-    }
     bool vertex = false;             // cached launches: this shading step reached a cache vertex
     Rng rng{0};
     Accum<F64> acc;
@@ -151,10 +145,10 @@ mega_kernel(RenderLaunch p) {
     // Samples with depth 0 finish immediately (the bounce loop never runs).
     auto start_samples = [&]() -> int {
         while (k < p.spp) {
-            if (CACHE && p.cache.sobol) {
-                // sample index since the last camera change (one pass per launch)
-                qseed = qmc_hash(gid + 1u);
-                qidx = (uint32_t)ci0 - 1u + stream + k;
+            if (CACHE && SOBOL) {
+                // the pixel's seed and the sample's index since the last camera
+                // change (one pass per launch: index = first pass - 1 + stream)
+                const uint32_t qseed = qmc_hash(gid + 1u), qidx = (uint32_t)ci0 - 1u + stream;
                 float ju, jv, l0, l1;
                 qmc_point(qseed, QMC_PIXEL, qidx, &ju, &jv);
                 qmc_point(qseed, QMC_LENS, qidx, &l0, &l1);
@@ -332,9 +326,22 @@ mega_kernel(RenderLaunch p) {
                                 const f3 a = surface_att();
                                 aclamp = mk(fmaxf(a.x, 1e-3f), fmaxf(a.y, 1e-3f), fmaxf(a.z, 1e-3f));
                                 vertex = true;
-                                if (p_train >= 1.0f || rng.f() < p_train) {
-                                    const uint32_t slot = atomicAdd(p.cache.train_count, 1u);
-                                    if (slot < p.cache.train_slots) tslot = slot;
+                                // trains with probability min(1, slots / vertices of
+                                // the previous frame), decided per group of 32 pixels
+                                // (a hash of group, frame and stream) so that a warp's
+                                // lanes mostly all train or all stop here
+                                const uint32_t prev = __ldg(p.cache.vertices_prev);
+                                const uint32_t coin = qmc_hash((gid >> 5) * 0x9e3779b9u ^
+                                                               p.cache.frame * 0x85ebca6bu ^ stream * 0xc2b2ae35u);
+                                if (prev <= p.cache.train_slots ||
+                                    (float)(coin >> 8) * (1.0f / 16777216.0f) * (float)prev < (float)p.cache.train_slots) {
+                                    // 32 counters, one per lane index, each owning a 32nd
+                                    // of the slots: a warp's lanes never wait on one
+                                    // address (train_slots is a multiple of 32)
+                                    const uint32_t shard = lane;
+                                    const uint32_t per = p.cache.train_slots >> 5;
+                                    const uint32_t slot = atomicAdd(p.cache.train_count + shard, 1u);
+                                    if (slot < per) tslot = shard * per + slot;
                                 }
                                 if (tslot == 0xffffffffu) {
                                     query = true;
@@ -354,8 +361,8 @@ mega_kernel(RenderLaunch p) {
                             if (nee) {
                                 const float target = rng.f() * p.cache.light_area;
                                 float u1, u2;
-                                if (p.cache.sobol && bounce == 0u) {
-                                    qmc_point(qseed, QMC_LIGHT, qidx, &u1, &u2);
+                                if (SOBOL && bounce == 0u) {
+                                    qmc_point(qmc_hash(gid + 1u), QMC_LIGHT, (uint32_t)ci0 - 1u + stream, &u1, &u2);
                                 } else {
                                     u1 = rng.f();
                                     u2 = rng.f();
@@ -413,9 +420,9 @@ mega_kernel(RenderLaunch p) {
                                     v2 = true;
                                     shadow_pre = shadow_ray;
                                 }
-                                const bool preset = p.cache.sobol && bounce == 0u;
+                                const bool preset = SOBOL && bounce == 0u;
                                 float pt = 0.0f, pp = 0.0f;
-                                if (preset) qmc_point(qseed, QMC_BOUNCE, qidx, &pt, &pp);
+                                if (preset) qmc_point(qmc_hash(gid + 1u), QMC_BOUNCE, (uint32_t)ci0 - 1u + stream, &pt, &pp);
                                 const bool cont = shade_geom<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, g, &ro, &rd, &color,
                                                                                &scn, preset, pt, pp);
                                 nee_prev = nee;
@@ -632,7 +639,7 @@ cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* 
 // ---- host-side launchers -----------------------------------------------------
 // Persistent grid: as many blocks as fit on the device at once (never more
 // than the pixels need).
-template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false>
+template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false, bool SOBOL = false>
 static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
     static int blocks_per_sm = 0, sms = 0;
     if (blocks_per_sm == 0) {
@@ -641,28 +648,37 @@ static cudaError_t launch_mega_tt(const RenderLaunch& p, cudaStream_t s) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 #ifdef ORN_MEGA_CARVEOUT
         // shared-memory share of the unified L1/shared space, in percent
-        cudaFuncSetAttribute(mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE>,
+        cudaFuncSetAttribute(mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE, SOBOL>,
                              cudaFuncAttributePreferredSharedMemoryCarveout, ORN_MEGA_CARVEOUT);
 #endif
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE, SOBOL>,
                                                       kMegaBlock, 0);
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
-    uint32_t need = (p.pixel_count + kMegaBlock - 1) / kMegaBlock;
+    const uint64_t items = CACHE ? (uint64_t)p.pixel_count * p.cache.streams : p.pixel_count;
+    uint32_t need = (uint32_t)((items + kMegaBlock - 1) / kMegaBlock);
     uint32_t grid = (uint32_t)(blocks_per_sm * sms);
     if (need < grid) grid = need;
     cudaError_t e = cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE><<<grid, kMegaBlock, 0, s>>>(p);
+    mega_kernel<SEM, MATH, COUNT, FAST, F64, CACHE, SOBOL><<<grid, kMegaBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 
-cudaError_t launch_mega_cached(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s) {
+// The Sobol sampler is a separate instantiation, so the stream sampler's
+// kernel carries none of its code.
+template <bool SOBOL>
+static cudaError_t launch_mega_cached_t(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s) {
     if (semantics == SEM_WGSL)
-        return fast ? launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, true, false, true>(p, s)
-                    : launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, false, false, true>(p, s);
-    return fast ? launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, true, false, true>(p, s)
-                : launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, false, false, true>(p, s);
+        return fast ? launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, true, false, true, SOBOL>(p, s)
+                    : launch_mega_tt<SEM_WGSL, MATH_PORTABLE, false, false, false, true, SOBOL>(p, s);
+    return fast ? launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, true, false, true, SOBOL>(p, s)
+                : launch_mega_tt<SEM_HIP, MATH_PORTABLE, false, false, false, true, SOBOL>(p, s);
+}
+
+cudaError_t launch_mega_cached(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s) {
+    return p.cache.sobol ? launch_mega_cached_t<true>(p, semantics, fast, s)
+                         : launch_mega_cached_t<false>(p, semantics, fast, s);
 }
 
 template <int SEM>

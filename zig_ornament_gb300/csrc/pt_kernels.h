@@ -51,6 +51,7 @@ constexpr int kCacheInputs = 10;   // position 3, direction 3, normal 3, roughne
 constexpr float kCacheMinFuzz = 0.25f;   // metals below this fuzz are not cache vertices
 
 struct CacheLaunch {
+    uint32_t frame;            // the cache's frame counter (training decisions)
     float lo[3];               // scene bounds: position inputs are (p - lo) * inv_extent
     float inv_extent[3];
     uint32_t* query_count;     // zeroed before the launch
@@ -62,9 +63,11 @@ struct CacheLaunch {
     uint32_t train_slots;      // capacity (all streams)
     // training paths are chosen at the cache vertex: a path that reaches one
     // trains with probability min(1, train_slots / *vertices_prev) (the
-    // previous frame's count of cache vertices) and takes the next slot from
-    // *train_count while there is one; *vertices counts this frame's vertices
-    uint32_t* train_count;     // zeroed before the launch
+    // previous frame's count of cache vertices) and takes the next free slot
+    // of its lane's shard (train_count[lane] counts slots taken from
+    // [shard * train_slots / 32, (shard + 1) * train_slots / 32)); *vertices
+    // counts this frame's vertices
+    uint32_t* train_count;     // [32], zeroed before the launch
     uint32_t* vertices;        // zeroed before the launch
     const uint32_t* vertices_prev;
     // next-event estimation: emissive mesh triangles, 4 float4 each (v0, e1,
