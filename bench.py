@@ -89,6 +89,9 @@ def parse():
     p.add_argument("--relmse-ref-spp", type=int, default=16384)
     p.add_argument("--relmse-budget", type=float, default=8.0, help="GPU seconds per method at most")
     p.add_argument("--frames", type=int, default=8, help="cached-frames: timed frames")
+    p.add_argument("--batched", action="store_true",
+                   help="cached-frames: the cached + batched configuration of the relMSE harness (8 sample "
+                        "streams, Sobol sampler, SAH tree, train_shift 3, lr 5e-3, 64 steps per frame)")
     p.add_argument("--scene", default="instanced", choices=["instanced", "closed-room"],
                    help="cached-frames: the scene")
     return p.parse_args()
@@ -587,16 +590,22 @@ def relmse_block(args):
 
 def run_cached_frames(args):
     """A profiling workload: --frames radiance-cache frames (after 4 warm-up
-    frames) of --scene at --width x --height."""
+    frames) of --scene at --width x --height; --batched for the cached +
+    batched configuration."""
     from zig_ornament_gb300 import _lib, ornament
     scene = relmse_scene(args.scene, args.width, args.height)
-    bvh = ornament.Bvh(scene, row_major_transforms=True)
+    bvh = ornament.Bvh(scene, row_major_transforms=True, builder="sah" if args.batched else "reference")
     r = ornament.Renderer(bvh, 0)
     r.set_resolution(args.width, args.height)
     st = ornament.State()
     st.depth = args.depth
     st.kernel = _lib.KERNEL_CACHED
-    cache = ornament.RadianceCache(seed=1)
+    cfg = {}
+    if args.batched:
+        st.spp_per_launch = 8
+        st.sampler = _lib.SAMPLER_SOBOL
+        cfg = {"train_shift": 3, "learning_rate": 5e-3, "steps_per_frame": 64}
+    cache = ornament.RadianceCache(seed=1, **cfg)
     r.attach_cache(cache)
     r.set_state(st.to_struct())
     r.set_camera(scene.camera.to_struct())
@@ -608,7 +617,8 @@ def run_cached_frames(args):
     r.render()
     r.synchronize()
     print(json.dumps({"mode": "cached-frames", "scene": args.scene, "width": args.width, "height": args.height,
-                      "frames": args.frames, "ms_per_frame": r.last_render_ms() / args.frames,
+                      "batched": bool(args.batched), "samples_per_frame": args.width * args.height * max(
+                          1, st.spp_per_launch), "frames": args.frames, "ms_per_frame": r.last_render_ms() / args.frames,
                       "cache": cache.stats()}), flush=True)
     r.attach_cache(None)
     r.close()

@@ -83,8 +83,11 @@ template <> struct Accum<true> {
 // first rough surface from the second vertex on) and leaves a query there; a
 // training pixel's path runs to the end and records the network inputs at
 // the cache vertex and the radiance that left it.
+#ifndef ORN_CACHE_MIN_BLOCKS
+#define ORN_CACHE_MIN_BLOCKS 4
+#endif
 template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false, bool SOBOL = false>
-__global__ void __launch_bounds__(kMegaBlock, CACHE ? 4 : kMegaMinBlocks)
+__global__ void __launch_bounds__(kMegaBlock, CACHE ? ORN_CACHE_MIN_BLOCKS : kMegaMinBlocks)
 mega_kernel(RenderLaunch p) {
     __shared__ uint32_t sstack[kSmemStack * kMegaBlock];
     TravStack<kSmemStack> stack;
@@ -278,8 +281,17 @@ mega_kernel(RenderLaunch p) {
                         if (mtype > ORN_DIELECTRIC) {
                             // emitter (or unknown type): the path ends with color x emission,
                             // unless the previous vertex sampled this emitter directly
-                            f3 c2 = color;
-                            shade_geom<SEM, MATH, COUNT>(p.scene, p.cp, rng, h, g, &ro, &rd, &c2, &scn);
+                            // (shade_geom's emission, computed here: a second inlined
+                            // copy of shade_geom cost instruction-cache misses)
+                            const uint32_t etex = bits(ma.w);
+                            const bool etex_on = SEM == SEM_WGSL
+                                                     ? (etex < p.cp.textures_count && etex < p.scene.textures_len)
+                                                     : etex < p.scene.textures_len;
+                            f3 em = mk(0.0f, 0.0f, 0.0f);
+                            if (mtype == ORN_DIFFUSE_LIGHT)
+                                em = etex_on ? tex_sample(p.scene.textures[etex], g.hu, g.hv, SEM == SEM_WGSL)
+                                             : mk(ma.x, ma.y, ma.z);
+                            f3 c2 = mul(color, em);
                             const bool sampled = nee_prev && h.type == ORN_NODE_MESH &&
                                                  __ldg(p.cache.light_material + h.material) != 0u;
                             if (sampled) {
