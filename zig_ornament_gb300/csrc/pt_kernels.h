@@ -140,7 +140,7 @@ constexpr int kShadeThreshold = ORN_SHADE_THRESHOLD;
 // BVH node visits a traversing lane makes per pass of the megakernel's loop
 // (amortises the loop's ballots).
 #ifndef ORN_STEPS_PER_ITERATION
-#define ORN_STEPS_PER_ITERATION 8
+#define ORN_STEPS_PER_ITERATION 32
 #endif
 constexpr int kStepsPerIteration = ORN_STEPS_PER_ITERATION;
 
