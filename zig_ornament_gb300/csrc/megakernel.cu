@@ -235,7 +235,8 @@ mega_kernel(RenderLaunch p) {
 #pragma unroll 1
             for (int s = 0; s < kStepsPerIteration; ++s) {
                 ++steps;
-                if (!walker_step<COUNT, kSmemStack, FAST>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon, &h, stack, &vc, &err)) {
+                if (!walker_step<COUNT, kSmemStack, FAST, CACHE>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon, &h, stack, &vc,
+                                                                 &err)) {
                     mode = LANE_SHADE;
                     break;
                 }
@@ -468,6 +469,9 @@ mega_kernel(RenderLaunch p) {
                                 rd = scale(cx2, ldir);
                                 walker_begin(w, p.scene, ro, rd);
                                 w.t_max = ldist / cx2 * (1.0f + 1e-3f);
+                                // any-hit: stop at an occluder before the light point
+                                w.occl_inv = shadow_inv;
+                                w.occl_t = ldist / cx2;
                                 shadow = true;
                                 mode = LANE_TRAVERSE;
                             }

@@ -39,6 +39,11 @@ struct Walker {
     float t_max;
     uint32_t material, inv_id;
     uint32_t visits;
+    // any-hit shadow rays (walker_step<..., ANY = true>): a hit before occl_t
+    // on an instance other than occl_inv ends the traversal (occluded);
+    // occl_inv = ~0 for ordinary rays
+    uint32_t occl_inv;
+    float occl_t;
 };
 
 __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 ro, f3 rd) {
@@ -47,6 +52,8 @@ __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 r
     w.blas_sp = 0;
     w.in_blas = false;
     w.any = false;
+    w.occl_inv = 0xffffffffu;
+    w.occl_t = 0.0f;
     w.o = ro;
     w.d = rd;
     w.inv = safe_invdir(rd);
@@ -68,7 +75,7 @@ __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 r
 // FAST selects the FMNMX slab test (aabb_hit_fast); the host decides per
 // render whether every ray of the render satisfies its condition
 // (render_fast_slabs in capi.cu).
-template <bool COUNT, int SS, bool FAST>
+template <bool COUNT, int SS, bool FAST, bool ANY = false>
 __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro, f3 rd, float t_min,
                                             HitRec* out, TravStack<SS>& stack, VisitCount* vc,
                                             uint32_t* err) {
@@ -121,6 +128,10 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
             out->tri = bits(a.w) * 3u;
             out->u = u;
             out->v = v;
+            if (ANY && w.occl_inv != 0xffffffffu && w.inv_id != w.occl_inv && t < w.occl_t) {
+                if (COUNT) vc->visits += w.visits;
+                return false;   // an occluder: the closest hit cannot be the sampled light
+            }
         }
     } else {
         float4 a, b, c, e;
@@ -155,6 +166,10 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
                 out->material = mat;
                 out->type = ORN_NODE_SPHERE;
                 out->inv = inv_index;
+                if (ANY && w.occl_inv != 0xffffffffu && t < w.occl_t) {
+                    if (COUNT) vc->visits += w.visits;
+                    return false;   // spheres never carry sampled lights
+                }
             }
         } else {
             if (COUNT) vc->mesh++;
