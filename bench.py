@@ -467,7 +467,7 @@ def relmse_scene(name, w, h):
 
 
 def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=None, warmup=64, methods=None,
-                   ref=None, streams=8, batched_warmup_spp=32, batched_sobol=True, batched_cfg=None):
+                   ref=None, streams=8, batched_warmup_spp=16, batched_sobol=True, batched_cfg=None):
     """GPU time each renderer needs to bring the relMSE against an FP64
     `ref_spp`-sample oracle (orn_render_f64) down to `target`: plain
     megakernel tracing, the cached renderer without the network (every pixel
@@ -477,7 +477,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
     the cached renderer itself), Adam lr 3e-3, 32 warm-up frames; and
     cached + batched: on the SAH tree, `streams` sample streams per pixel
     batched into each frame's launch (orn_state.spp_per_launch), the Sobol
-    sampler, training slots for 1/8 of the samples at lr 5e-3, a 32-sample
+    sampler, training slots for 1/8 of the samples at lr 5e-3, a 16-sample
     warm-up.  Progressive rendering
     in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
     chunks outside the timed renders; the crossing is interpolated
