@@ -610,6 +610,7 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     const uint32_t steps = std::min(c->config.steps_per_frame, nb);
     p.do_post = 0;
     p.spp = 1;
+    p.shade_threshold = orn::kCacheShadeThreshold;
     const uint32_t streams = ctx->cq_streams;
     p.cache.streams = streams;
     p.cache.rng_extra = ctx->rng_extra;

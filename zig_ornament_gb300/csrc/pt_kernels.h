@@ -137,6 +137,11 @@ cudaError_t launch_pixel_order(const PixelOrder& o, cudaStream_t s);
 #define ORN_SHADE_THRESHOLD 8
 #endif
 constexpr int kShadeThreshold = ORN_SHADE_THRESHOLD;
+// the cached kernel's (its shading step is several times longer)
+#ifndef ORN_CACHE_SHADE_THRESHOLD
+#define ORN_CACHE_SHADE_THRESHOLD 16
+#endif
+constexpr int kCacheShadeThreshold = ORN_CACHE_SHADE_THRESHOLD;
 // BVH node visits a traversing lane makes per pass of the megakernel's loop
 // (amortises the loop's ballots).
 #ifndef ORN_STEPS_PER_ITERATION
