@@ -553,7 +553,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             curve.append((t, n, e))
             if e <= target or t >= budget_s:
                 break
-            chunk = min(chunk * 2, 1024)
+            chunk = min(max(chunk + 1, chunk * 3 // 2), 1024)   # x1.5: finer readings near the target
         reached = curve[-1][2] <= target
         if reached and len(curve) > 1:
             (ta, _, ea), (tb, _, eb) = curve[-2], curve[-1]
