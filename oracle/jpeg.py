@@ -1,5 +1,5 @@
 """float64 numpy restatement of the pixel stage of JPEG decoding — test
-infrastructure (the checker of zig_ornament_gb300/csrc/jpeg.cu).
+infrastructure: the oracle for zig_ornament_gb300/csrc/jpeg.cu.
 
 From quantised coefficient planes (natural order, as the entropy decoder
 returns them and as tests/golden/make_jpeg.py wrote them): dequantise, exact

@@ -1,6 +1,6 @@
 """FP64 numpy restatement of the radiance-cache network — test infrastructure.
 
-The checker for the tensor-core MLP kernels (zig_ornament_gb300/csrc/
+The oracle for the tensor-core MLP kernels (zig_ornament_gb300/csrc/
 radiance_cache.cu): the same encoding, layer shapes, loss and Adam update,
 in float64.  The reference renderer has no learned cache; this network is an
 extension, so there is no reference file to follow — the oracle states the
