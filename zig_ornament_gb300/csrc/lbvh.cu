@@ -71,7 +71,7 @@ __global__ void hierarchy_kernel(const unsigned long long* __restrict__ keys, in
     const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
     const int dmin = delta(keys, n, i, i - d);
     int lmax = 2;
-    while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+    while (lmax < n && delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;   // (the bound keeps i + lmax*d from overflowing)
     int l = 0;
     for (int t = lmax / 2; t >= 1; t /= 2)
         if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
@@ -218,6 +218,7 @@ __global__ void write_kernel(const float* __restrict__ tri, const unsigned long 
 int lbvh_build_blas(const float* tri_host, uint32_t n, uint32_t first_global, uint32_t node_offset,
                     orn_bvh_node* out_host) {
     if (n == 0) return ORN_ERR_EMPTY_SCENE;
+    if (n >= (1u << 31)) return ORN_ERR_INVALID_ARGUMENT;   // node and sort indices are int
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return ORN_ERR_NO_DEVICE;
     if (n == 1) {
