@@ -583,6 +583,14 @@ int orn_bvh_get_blob(const orn_bvh* bvh, orn_scene_blob* blob);
 /* Bvh.deinit — src/bvh.zig:80-90. */
 int orn_bvh_free(orn_bvh* bvh);
 
+/* Parity / debugging (host only): points of the cached kernel's Sobol
+ * sampler (orn_state.sampler = ORN_SAMPLER_SOBOL) — `count` 2-D points of
+ * use `pair` (0 pixel jitter, 1 lens, 2 first-bounce direction, 3 first
+ * light sample) for the pixel with index `pixel`, sample indices `first` ..
+ * first + count - 1, exactly as the kernel computes them (the same inline
+ * code); `out` receives 2 * count floats in [0, 1). */
+int orn_qmc_points(uint32_t pixel, uint32_t pair, uint32_t first, uint32_t count, float* out);
+
 /* ---- JPEG textures -------------------------------------------------------
  * The example app loads its textures with zstbi (stb_image) as 4-component
  * RGBA8 images flipped vertically on load (glfw_example/examples.zig:492-503

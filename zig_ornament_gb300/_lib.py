@@ -219,6 +219,7 @@ FUNCTIONS = {
     "orn_jpeg_coefficients": (C.c_int, [_P, C.c_size_t, C.c_uint32, _P, C.c_size_t, C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32), _P]),
     "orn_jpeg_last_error": (C.c_char_p, []),
+    "orn_qmc_points": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
 }
 
 _lib = None

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "ornament_cuda.h"
+#include "qmc.cuh"
 #include "pt_kernels.h"
 #include "batch.h"
 #include "rc_host.h"
@@ -751,6 +752,13 @@ uint32_t orn_abi_version(void) { return ORN_ABI_VERSION; }
 int orn_get_device(const orn_context* ctx, int* device) {
     if (!ctx || !device) return ORN_ERR_INVALID_ARGUMENT;
     *device = ctx->device;
+    return ORN_OK;
+}
+
+int orn_qmc_points(uint32_t pixel, uint32_t pair, uint32_t first, uint32_t count, float* out) {
+    if (!out || pair > orn::QMC_LIGHT) return ORN_ERR_INVALID_ARGUMENT;
+    const uint32_t seed = orn::qmc_hash(pixel + 1u);   // the cached kernel's pixel seed
+    for (uint32_t k = 0; k < count; ++k) orn::qmc_point(seed, pair, first + k, out + 2 * (size_t)k, out + 2 * (size_t)k + 1);
     return ORN_OK;
 }
 

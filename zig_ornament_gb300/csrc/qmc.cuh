@@ -21,7 +21,20 @@ namespace orn {
 
 enum QmcPair { QMC_PIXEL = 0, QMC_LENS = 1, QMC_BOUNCE = 2, QMC_LIGHT = 3 };
 
-__device__ __forceinline__ uint32_t qmc_hash(uint32_t x) {
+// Host and device (the host copy serves the orn_qmc_points check).
+__host__ __device__ __forceinline__ uint32_t qmc_brev(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __brev(x);
+#else
+    x = ((x >> 1) & 0x55555555u) | ((x & 0x55555555u) << 1);
+    x = ((x >> 2) & 0x33333333u) | ((x & 0x33333333u) << 2);
+    x = ((x >> 4) & 0x0f0f0f0fu) | ((x & 0x0f0f0f0fu) << 4);
+    x = ((x >> 8) & 0x00ff00ffu) | ((x & 0x00ff00ffu) << 8);
+    return (x >> 16) | (x << 16);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t qmc_hash(uint32_t x) {
     // integer finaliser (xorshift-multiply), a seed mixer only
     x ^= x >> 16;
     x *= 0x7feb352du;
@@ -32,7 +45,7 @@ __device__ __forceinline__ uint32_t qmc_hash(uint32_t x) {
 }
 
 // Laine-Karras style permutation of the reversed bits (Burley 2020, eq. 2).
-__device__ __forceinline__ uint32_t qmc_lk_permute(uint32_t x, uint32_t seed) {
+__host__ __device__ __forceinline__ uint32_t qmc_lk_permute(uint32_t x, uint32_t seed) {
     x += seed;
     x ^= x * 0x6c50b47cu;
     x ^= x * 0xb82f1e52u;
@@ -41,11 +54,11 @@ __device__ __forceinline__ uint32_t qmc_lk_permute(uint32_t x, uint32_t seed) {
     return x;
 }
 
-__device__ __forceinline__ uint32_t qmc_owen(uint32_t x, uint32_t seed) {
-    return __brev(qmc_lk_permute(__brev(x), seed));
+__host__ __device__ __forceinline__ uint32_t qmc_owen(uint32_t x, uint32_t seed) {
+    return qmc_brev(qmc_lk_permute(qmc_brev(x), seed));
 }
 
-__device__ __forceinline__ uint32_t qmc_sobol1(uint32_t i) {
+__host__ __device__ __forceinline__ uint32_t qmc_sobol1(uint32_t i) {
     uint32_t v = 0u, c = 0x80000000u;
     for (; i != 0u; i >>= 1) {
         if (i & 1u) v ^= c;
@@ -55,10 +68,11 @@ __device__ __forceinline__ uint32_t qmc_sobol1(uint32_t i) {
 }
 
 // Point `pair` of sample `index` of the pixel whose seed is `pixel_seed`.
-__device__ __forceinline__ void qmc_point(uint32_t pixel_seed, uint32_t pair, uint32_t index, float* u0, float* u1) {
+__host__ __device__ __forceinline__ void qmc_point(uint32_t pixel_seed, uint32_t pair, uint32_t index, float* u0,
+                                                   float* u1) {
     const uint32_t s = qmc_hash(pixel_seed ^ (0x9e3779b9u * (pair + 1u)));
     const uint32_t i = qmc_owen(index, s);
-    const uint32_t x = qmc_owen(__brev(i), qmc_hash(s ^ 0x68bc21ebu));
+    const uint32_t x = qmc_owen(qmc_brev(i), qmc_hash(s ^ 0x68bc21ebu));
     const uint32_t y = qmc_owen(qmc_sobol1(i), qmc_hash(s ^ 0x02e5be93u));
     *u0 = (float)(x >> 8) * (1.0f / 16777216.0f);
     *u1 = (float)(y >> 8) * (1.0f / 16777216.0f);
