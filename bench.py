@@ -26,6 +26,14 @@ kernels) on the same workload sample; it runs on rank 0 only.
 Multi-GPU: one process per GPU (torchrun); every rank renders its own copy
 of the frame (replicas: pixels and samples are independent, no exchange);
 value = all ranks' samples / the slowest rank's time.
+
+The headline line also carries the same steps on the non-parity trees
+(`sah_tree`, `lbvh_tree`) and the time-to-relMSE block (plain megakernel
+against the cached renderers, two scenes at 640x360).  Other modes:
+`--workload spheres|large`, `--bvh sah|lbvh`, `--mode relmse` (the block
+alone), `--mode batch` (64 scenes in one graph-replayed launch against
+sequential launches), `--mode cached-frames [--batched]` (a profiling
+workload of radiance-cache frames).
 """
 from __future__ import annotations
 
