@@ -191,11 +191,11 @@ bool decode_block(Bits& br, const Huffman& dc, const Huffman& ac, int* pred, int
 }
 
 struct Parser {
-    const uint8_t* data;
-    size_t len;
+    const uint8_t* data = nullptr;
+    size_t len = 0;
     size_t pos = 0;
-    Image* img;
-    std::string* err;
+    Image* img = nullptr;
+    std::string* err = nullptr;
     Huffman dc[4], ac[4];
     uint32_t restart = 0;
     bool have_frame = false;
@@ -444,7 +444,11 @@ std::string& last_error() {
 int parse(const uint8_t* data, size_t len, bool header_only, Image* out, std::string* err) {
     if (!data || !out) return ORN_ERR_INVALID_ARGUMENT;
     *out = Image{};
-    Parser ps{data, len, 0, out, err};
+    Parser ps;
+    ps.data = data;
+    ps.len = len;
+    ps.img = out;
+    ps.err = err;
     return ps.run(header_only);
 }
 
