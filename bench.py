@@ -474,6 +474,22 @@ def relmse_scene(name, w, h):
     return scenes.instanced_meshes_scene(w, h, n_lights=3)
 
 
+def crossing_time(curve, target):
+    """(seconds, reached) at which a progressive render's relMSE reaches
+    `target`, from readings [(seconds, samples, relMSE), ...]: log-linear
+    between the two readings around the crossing, the first reading if it is
+    already below, or extrapolated as relMSE ~ 1/time when never reached."""
+    import math
+    reached = curve[-1][2] <= target
+    if reached and len(curve) > 1:
+        (ta, _, ea), (tb, _, eb) = curve[-2], curve[-1]
+        f = (math.log(ea) - math.log(target)) / max(math.log(ea) - math.log(eb), 1e-12)
+        return math.exp(math.log(ta) + f * (math.log(tb) - math.log(ta))), True
+    if reached:
+        return curve[-1][0], True
+    return curve[-1][0] * curve[-1][2] / target, False
+
+
 def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=None, warmup=64, methods=None,
                    ref=None, streams=8, batched_warmup_spp=16, batched_sobol=True, batched_cfg=None):
     """GPU time each renderer needs to bring the relMSE against an FP64
@@ -490,8 +506,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
     in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
     chunks outside the timed renders; the crossing is interpolated
     log-linearly between the two chunks around it, or extrapolated as
-    relMSE ~ 1/time past the budget."""
-    import math
+    relMSE ~ 1/time past the budget (crossing_time)."""
     from zig_ornament_gb300 import _lib, ornament
 
     scene = relmse_scene(name, w, h)
@@ -562,15 +577,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             if e <= target or t >= budget_s:
                 break
             chunk = min(max(chunk + 1, chunk * 3 // 2), 1024)   # x1.5: finer readings near the target
-        reached = curve[-1][2] <= target
-        if reached and len(curve) > 1:
-            (ta, _, ea), (tb, _, eb) = curve[-2], curve[-1]
-            f = (math.log(ea) - math.log(target)) / max(math.log(ea) - math.log(eb), 1e-12)
-            tt = math.exp(math.log(ta) + f * (math.log(tb) - math.log(ta)))
-        elif reached:
-            tt = curve[-1][0]
-        else:
-            tt = curve[-1][0] * curve[-1][2] / target   # relMSE ~ 1/time
+        tt, reached = crossing_time(curve, target)
         out[method] = {"seconds": round(tt, 4), "reached": reached,
                        "samples_per_pixel": n, "final_relmse": curve[-1][2],
                        "curve": [[round(a, 4), b, float("%.4g" % c)] for a, b, c in curve]}

@@ -28,3 +28,17 @@ def test_reference_arm_line():
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert d["config"]["resolution"] == "1920x1080"
+
+
+def test_relmse_crossing_time():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    # relMSE falling as 1/time: the crossing of 1e-3 is at exactly 2 s
+    curve = [(0.5, 16, 4e-3), (1.0, 32, 2e-3), (4.0, 128, 5e-4)]
+    t, reached = bench.crossing_time(curve, 1e-3)
+    assert reached and abs(t - 2.0) < 1e-9
+    # below the target at the first reading
+    assert bench.crossing_time([(0.3, 16, 5e-4)], 1e-3) == (0.3, True)
+    # never reached: extrapolated as relMSE ~ 1/time
+    t, reached = bench.crossing_time([(1.0, 16, 4e-3), (2.0, 32, 2e-3)], 1e-3)
+    assert not reached and abs(t - 4.0) < 1e-9
