@@ -315,7 +315,8 @@ int orn_get_stream(const orn_context* ctx, void** stream);
 int orn_launch_count(const orn_context* ctx, uint64_t* launches);
 
 /* ---- FP64 reference and error -------------------------------------------
- * The image-quality oracle of SURVEY's configurations: `spp` passes from a
+ * The image-quality oracle of the time-to-relMSE measurements (an
+ * extension: the reference has no error metric): `spp` passes from a
  * fresh start (RNG seeded with the pixel index, current_iteration 1..spp)
  * with the context's resolution, State and camera, accumulated in FP64 on
  * the GPU (the only FP64 in the renderer besides the error reduction);
@@ -362,16 +363,26 @@ int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int swap_offsets, const ui
  * per pixel) are device buffers read and updated in place (seed a fresh
  * render with rng_state[i] = i); `framebuffer` (float4 per pixel) is a
  * device buffer written.  Work is queued on `stream` (a cudaStream_t; NULL
- * is the default stream) and the call returns without waiting; device-side
- * errors surface at the context's next orn_synchronize.  Results are
- * bit-identical to orn_render with the same state.
+ * is the default stream) and the call returns without waiting, so a frame
+ * loop is never blocked by it.  A device-side limit hit by a render (a ray
+ * needing more than 64 stack entries or 2^24 node visits) is recorded in
+ * the context's error word; each call queues a copy of that word into
+ * pinned host memory (allocated by orn_create) behind its work, and the next
+ * call, once that copy has arrived, returns ORN_ERR_STACK_OVERFLOW /
+ * ORN_ERR_TIMEOUT without queuing anything and clears the word.
+ * orn_synchronize(ctx) reports it too (and waits).  Results are
+ * bit-identical to orn_render with the same state.  The work runs on the
+ * context's device; the caller's current device is restored on return.
  *
  * Returns ORN_ERR_INVALID_ARGUMENT when width * height exceeds
- * ORN_NOALLOC_MAX_PIXELS or a pointer is NULL.  The first call on each device
- * looks up the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture.  All calls share the one array, so
- * calls whose GPU work overlaps (other streams, other threads) race. */
+ * ORN_NOALLOC_MAX_PIXELS, depth exceeds ORN_NOALLOC_MAX_DEPTH (the call
+ * queues spp * (depth + 1) + 2 kernel pairs, bounded by these limits) or a
+ * pointer is NULL.  The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the one array, so calls whose GPU work
+ * overlaps (other streams, other threads) race. */
 #define ORN_NOALLOC_MAX_PIXELS 131072u
+#define ORN_NOALLOC_MAX_DEPTH 64u
 int orn_render_noalloc(const orn_context* ctx, const orn_constant_params* params, uint32_t spp,
                        float* accumulation, uint32_t* rng_state, float* framebuffer, void* stream);
 

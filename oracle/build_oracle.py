@@ -6,7 +6,14 @@ ORN_REFERENCE_DIR, default /root/reference), the reference's own HIP kernel
 source is compiled unmodified through oracle/shim into
 oracle/_ref/libref_libm.so (glibc transcendentals) and
 oracle/_ref/libref_pmath.so (the project's portable transcendentals).
-Both use -ffp-contract=off: no multiply-add contraction, as on the GPU.
+All three use the same flags: -O3 -ffp-contract=off -fno-fast-math (no
+multiply-add contraction, as on the GPU) with OpenMP, so the restatement and
+the reference's code are timed on equal terms.  No -march/-mcpu=native: the
+same objects must give the same bits on x86-64 and aarch64 hosts.
+
+This recipe is the one place that names where the reference sources are
+looked for: ORN_REFERENCE_DIR when set, else the checkout location of the
+build container.
 """
 from __future__ import annotations
 
@@ -24,7 +31,7 @@ REF_PMATH = REF_OUT / "libref_pmath.so"
 REFERENCE_DIR = Path(os.environ.get("ORN_REFERENCE_DIR", "/root/reference"))
 REF_KERNELS = REFERENCE_DIR / "src" / "hip_backend" / "kernels"
 
-FLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+FLAGS = ["-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
          f"-I{ROOT / 'include'}", f"-I{ROOT / 'zig_ornament_gb300' / 'csrc'}"]
 
 

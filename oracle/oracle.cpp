@@ -4,8 +4,8 @@
 // (its CPU-baseline leg and the reference arm) load the library built from
 // this file; the product never does.  It is pinned bit-for-bit against the
 // reference's own HIP kernels compiled for the host (oracle/ref_driver.cpp)
-// in tests/test_oracle_pin.py and against committed golden vectors in
-// tests/golden/.
+// (tests/test_oracle_golden.py::test_oracle_matches_compiled_reference)
+// and against committed golden vectors in tests/golden/.
 //
 // Every function follows the reference's arithmetic in the same operation
 // order (no FMA contraction: build with -ffp-contract=off), citing the

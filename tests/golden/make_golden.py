@@ -1,7 +1,7 @@
 """Generates tests/golden/golden_v1.npz from the reference itself.
 
-Run in a checkout where the zig_ornament sources are available (the path in
-ORN_REFERENCE_DIR, default /root/reference):
+Run where the zig_ornament sources are available (the directory
+oracle/build_oracle.py looks in; ORN_REFERENCE_DIR overrides it):
 
     python tests/golden/make_golden.py
 

@@ -94,4 +94,32 @@ def test_noalloc_rejects_oversized_frames():
     assert 1024 * 1024 > _lib.NOALLOC_MAX_PIXELS
     st = lib.orn_render_noalloc(r.handle, C.byref(cp), 1, 16, 16, 16, None)
     assert st == 1                            # ORN_ERR_INVALID_ARGUMENT, nothing launched
+    cp = r.peek_constant_params()
+    cp.depth = _lib.NOALLOC_MAX_DEPTH + 1     # the call would queue spp * (depth + 1) + 2 launch pairs
+    st = lib.orn_render_noalloc(r.handle, C.byref(cp), 1, 16, 16, 16, None)
+    assert st == 1
+    r.close()
+
+
+def test_noalloc_keeps_the_callers_device():
+    import torch
+    lib = _lib.load()
+    scene = scenes.small_test_scene(W, H)
+    r = ornament.Renderer(ornament.Bvh(scene), device=0)
+    r.set_resolution(W, H)
+    r.set_state(state(1))
+    r.set_camera(scene.camera.to_struct())
+    cp = r.peek_constant_params()
+    dev = torch.device("cuda", 0)
+    acc = torch.zeros((W * H, 4), dtype=torch.float32, device=dev)
+    rng = torch.arange(W * H, dtype=torch.int32, device=dev)
+    fb = torch.zeros((W * H, 4), dtype=torch.float32, device=dev)
+    before = torch.cuda.current_device()
+    for _ in range(3):   # later calls also read the previous call's error report
+        st = lib.orn_render_noalloc(r.handle, C.byref(cp), 1, acc.data_ptr(), rng.data_ptr(), fb.data_ptr(),
+                                    torch.cuda.current_stream(dev).cuda_stream)
+        assert st == 0, lib.orn_status_string(st)
+        torch.cuda.synchronize(dev)
+    assert torch.cuda.current_device() == before
+    r.synchronize()
     r.close()

@@ -28,6 +28,7 @@ SEMANTICS_HIP, SEMANTICS_WGSL = 0, 1
 KERNEL_MEGA, KERNEL_WAVEFRONT = 0, 1
 COUNTER_COUNT = 10
 NOALLOC_MAX_PIXELS = 131072
+NOALLOC_MAX_DEPTH = 64
 CACHE_INPUTS = 10
 CACHE_OUTPUTS = 3
 CACHE_PARAM_COUNT = 33792

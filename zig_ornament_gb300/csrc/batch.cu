@@ -354,6 +354,12 @@ int launch_frame(orn_batch* b, uint32_t nviews, uint32_t total, uint32_t sem, bo
 }
 
 // ---- autotuner cache: {"<key>": {"block": B, "blocks_per_sm": N, "shade_threshold": T, "ms": X}, ...}
+// The launch configurations the batched kernel is compiled for.
+bool valid_config(int block, int blocks_per_sm, int shade_threshold) {
+    return (block == 64 || block == 128 || block == 192) && blocks_per_sm >= 1 && blocks_per_sm <= 32 &&
+           shade_threshold >= 1 && shade_threshold <= 32;
+}
+
 std::map<std::string, orn::BatchConfig> read_cache(const char* path) {
     std::map<std::string, orn::BatchConfig> out;
     if (!path) return out;
@@ -386,8 +392,11 @@ std::map<std::string, orn::BatchConfig> read_cache(const char* path) {
         if (cb == std::string::npos) break;
         const std::string obj = s.substr(ob, cb - ob + 1);
         orn::BatchConfig c{};
+        // an entry outside the launchable range (a hand-edited or foreign
+        // file) is dropped: its workload is tuned again
         if (num(obj, "block", &c.block) && num(obj, "blocks_per_sm", &c.blocks_per_sm) &&
-            num(obj, "shade_threshold", &c.shade_threshold))
+            num(obj, "shade_threshold", &c.shade_threshold) &&
+            valid_config(c.block, c.blocks_per_sm, c.shade_threshold))
             out[key] = c;
         pos = cb + 1;
     }
@@ -527,8 +536,7 @@ int orn_batch_get_config(const orn_batch* b, orn_batch_config* out) {
 
 int orn_batch_set_config(orn_batch* b, const orn_batch_config* c) {
     if (!b || !c) return ORN_ERR_INVALID_ARGUMENT;
-    if ((c->block != 64 && c->block != 128 && c->block != 192) || c->blocks_per_sm < 1 || c->blocks_per_sm > 32 ||
-        c->shade_threshold < 1 || c->shade_threshold > 32)
+    if (!valid_config((int)c->block, (int)c->blocks_per_sm, (int)c->shade_threshold))
         return bfail(b, ORN_ERR_INVALID_ARGUMENT, "invalid batch launch configuration");
     b->config = orn::BatchConfig{(int)c->block, (int)c->blocks_per_sm, (int)c->shade_threshold};
     return ORN_OK;

@@ -65,6 +65,13 @@ struct orn_context {
 
     uint32_t* d_error = nullptr;
     uint32_t* d_work = nullptr;
+    // orn_render_noalloc's report of device-side errors without waiting: a
+    // pinned copy of d_error queued after its work, the event recorded after
+    // that copy, and whether a copy is outstanding (mutable: that entry point
+    // takes a const context)
+    mutable uint32_t* na_host_error = nullptr;
+    mutable cudaEvent_t na_done = nullptr;
+    mutable bool na_pending = false;
     // wavefront path pool (allocated on first use)
     uint32_t wf_slots = 0;
     std::vector<void*> wf_allocs;
@@ -677,14 +684,18 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
 namespace orn {
 
 // For orn_render_noalloc (noalloc.cu): the device-resident scene of a
-// context and what a render with `camera` needs to launch the wavefront
-// (the FMNMX slab condition is render_fast_slabs' check for that camera).
-const SceneDev* context_scene(const orn_context* ctx, int* device, uint32_t* semantics, uint32_t** error_word,
-                              bool* fast_slabs, const orn_camera* camera) {
-    if (!ctx || !camera) return nullptr;
-    *device = ctx->device;
-    *semantics = ctx->state.semantics;
-    *error_word = ctx->d_error;
+// context, what a render with `camera` needs to launch the wavefront (the
+// FMNMX slab condition is render_fast_slabs' check for that camera), and the
+// context's error word with its pinned copy.
+bool noalloc_link(const orn_context* ctx, const orn_camera* camera, NoAllocLink* out) {
+    if (!ctx || !camera || !out || !ctx->na_host_error || !ctx->na_done) return false;
+    out->scene = &ctx->scene;
+    out->device = ctx->device;
+    out->semantics = ctx->state.semantics;
+    out->error_word = ctx->d_error;
+    out->host_error = ctx->na_host_error;
+    out->done = &ctx->na_done;
+    out->pending = &ctx->na_pending;
     bool fast = !ctx->scene.exact_slabs;
     double s = ctx->world_extent;
     for (int i = 0; i < 3 && fast; ++i) {
@@ -696,8 +707,8 @@ const SceneDev* context_scene(const orn_context* ctx, int* device, uint32_t* sem
     }
     if (fast && !(s < 1e29)) fast = false;
     if (fast && !(4.0 * ctx->max_inverse_entry * (s + 1.0) < 1e29)) fast = false;
-    *fast_slabs = fast;
-    return &ctx->scene;
+    out->fast_slabs = fast;
+    return true;
 }
 
 int batch_prepare(orn_context* ctx, BatchView* view, bool* fast_slabs, uint32_t* semantics, int* device,
@@ -806,6 +817,9 @@ int orn_create(const orn_scene_blob* blob, int device, orn_context** out) {
         ORN_CUDA(ctx, cudaMalloc(&ctx->d_error, 4));
         ORN_CUDA(ctx, cudaMemset(ctx->d_error, 0, 4));
         ORN_CUDA(ctx, cudaMalloc(&ctx->d_work, 4));
+        ORN_CUDA(ctx, cudaMallocHost(&ctx->na_host_error, 4));
+        *ctx->na_host_error = 0;
+        ORN_CUDA(ctx, cudaEventCreateWithFlags(&ctx->na_done, cudaEventDisableTiming));
         ORN_CUDA(ctx, cudaMalloc(&ctx->d_counters, ORN_COUNTER_COUNT * sizeof(unsigned long long)));
         ORN_CUDA(ctx, cudaMemset(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long)));
         std::vector<float4> nodes;
@@ -950,6 +964,8 @@ int orn_destroy(orn_context* ctx) {
         if (e) cudaEventDestroy(e);
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_work) cudaFree(ctx->d_work);
+    if (ctx->na_host_error) cudaFreeHost(ctx->na_host_error);
+    if (ctx->na_done) cudaEventDestroy(ctx->na_done);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     free_cache_buffers(ctx);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);

@@ -16,6 +16,11 @@
 // any stream capture.  Every call shares the one array: the call clears the
 // parts that must start at zero, and calls whose work overlaps on the GPU
 // (different streams, or another thread) race on it.
+//
+// The call never waits for the GPU: device-side errors of one call are
+// reported by the next (through a pinned copy of the context's error word
+// that each call queues behind its work), and the caller's current device
+// is restored before returning.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -70,32 +75,67 @@ cudaError_t scratch_address(int device, unsigned char** out) {
 
 }  // namespace
 
-// The scene of a context (capi.cu); declared here to keep the context type
-// private to capi.cu.
 namespace orn {
-const SceneDev* context_scene(const orn_context* ctx, int* device, uint32_t* semantics, uint32_t** error_word,
-                              bool* fast_slabs, const orn_camera* camera);
+bool noalloc_link(const orn_context* ctx, const orn_camera* camera, NoAllocLink* out);
 }
+
+namespace {
+
+// Restores the caller's current device when the call returns.
+struct DeviceRestore {
+    int device = -1;
+    ~DeviceRestore() {
+        if (device >= 0) cudaSetDevice(device);
+    }
+};
+
+int status_of(uint32_t err) {
+    return (err & orn::ERR_STACK) ? ORN_ERR_STACK_OVERFLOW : ORN_ERR_TIMEOUT;
+}
+
+}  // namespace
 
 extern "C" int orn_render_noalloc(const orn_context* ctx, const orn_constant_params* params, uint32_t spp,
                                   float* accumulation, uint32_t* rng_state, float* framebuffer, void* stream) {
     if (!ctx || !params || !accumulation || !rng_state || !framebuffer || spp == 0) return ORN_ERR_INVALID_ARGUMENT;
     const uint64_t pixels = (uint64_t)params->width * params->height;
     if (pixels == 0 || pixels > kNoAllocMaxPixels) return ORN_ERR_INVALID_ARGUMENT;
-    int device = 0;
-    uint32_t semantics = 0;
-    uint32_t* error_word = nullptr;
-    bool fast = false;
-    const orn::SceneDev* scene = orn::context_scene(ctx, &device, &semantics, &error_word, &fast, &params->camera);
-    if (!scene || device < 0 || device >= kMaxDevices) return ORN_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(device) != cudaSuccess) return ORN_ERR_CUDA;
+    if (params->depth > ORN_NOALLOC_MAX_DEPTH) return ORN_ERR_INVALID_ARGUMENT;
+    orn::NoAllocLink link;
+    if (!orn::noalloc_link(ctx, &params->camera, &link) || link.device < 0 || link.device >= kMaxDevices)
+        return ORN_ERR_INVALID_ARGUMENT;
+    int caller_device = -1;
+    if (cudaGetDevice(&caller_device) != cudaSuccess) return ORN_ERR_CUDA;
+    DeviceRestore restore;
+    if (caller_device != link.device) {
+        if (cudaSetDevice(link.device) != cudaSuccess) return ORN_ERR_CUDA;
+        restore.device = caller_device;
+    }
     unsigned char* base = nullptr;
-    if (scratch_address(device, &base) != cudaSuccess) return ORN_ERR_CUDA;
+    if (scratch_address(link.device, &base) != cudaSuccess) return ORN_ERR_CUDA;
     cudaStream_t s = (cudaStream_t)stream;
+
+    // A device-side limit hit by the previous call's work (or any other work
+    // of the context): reported once the pinned copy queued after that work
+    // has arrived, without waiting for it.
+    if (*link.pending) {
+        const cudaError_t q = cudaEventQuery(*link.done);
+        if (q == cudaSuccess) {
+            *link.pending = false;
+            const uint32_t err = *link.host_error;
+            if (err) {
+                *link.host_error = 0;
+                if (cudaMemsetAsync(link.error_word, 0, sizeof(uint32_t), s) != cudaSuccess) return ORN_ERR_CUDA;
+                return status_of(err);
+            }
+        } else if (q != cudaErrorNotReady) {
+            return ORN_ERR_CUDA;
+        }
+    }
 
     orn::WaveLaunch w;
     std::memset(&w, 0, sizeof(w));
-    w.scene = *scene;
+    w.scene = *link.scene;
     w.cp = *params;
     w.spp = spp;
     w.do_post = 1;
@@ -104,7 +144,7 @@ extern "C" int orn_render_noalloc(const orn_context* ctx, const orn_constant_par
     w.acc = (float4*)accumulation;
     w.fb = (float4*)framebuffer;
     w.rng = rng_state;
-    w.error = error_word;
+    w.error = link.error_word;
     w.counters = nullptr;
     w.pixel_counter = (uint32_t*)(base + kOffCounters);
     w.qstat = (uint32_t*)(base + kOffCounters) + 4;
@@ -129,9 +169,14 @@ extern "C" int orn_render_noalloc(const orn_context* ctx, const orn_constant_par
     // the last ray find an empty queue and return at once).  No readback.
     const uint64_t iterations = (uint64_t)spp * ((uint64_t)params->depth + 1) + 2;
     for (uint64_t it = 0; it < iterations; ++it) {
-        if (orn::launch_wf_logic(w, (uint32_t)it, (int)semantics, orn::MATH_PORTABLE, false, s) != cudaSuccess)
+        if (orn::launch_wf_logic(w, (uint32_t)it, (int)link.semantics, orn::MATH_PORTABLE, false, s) != cudaSuccess)
             return ORN_ERR_CUDA;
-        if (orn::launch_wf_extend(w, (uint32_t)it, false, fast, s) != cudaSuccess) return ORN_ERR_CUDA;
+        if (orn::launch_wf_extend(w, (uint32_t)it, false, link.fast_slabs, s) != cudaSuccess) return ORN_ERR_CUDA;
     }
+    // the error word after this call's work, for the next call to report
+    if (cudaMemcpyAsync(link.host_error, link.error_word, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return ORN_ERR_CUDA;
+    if (cudaEventRecord(*link.done, s) != cudaSuccess) return ORN_ERR_CUDA;
+    *link.pending = true;
     return ORN_OK;
 }

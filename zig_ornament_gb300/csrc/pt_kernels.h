@@ -114,6 +114,22 @@ struct RenderLaunch {
     uint32_t* cost;            // per-pixel traversal steps of this launch (or null)
 };
 
+// What orn_render_noalloc (noalloc.cu) takes from a context (capi.cu keeps
+// the context type private): its scene, device and semantics, whether the
+// FMNMX slab test may be used with the call's camera, the device error word,
+// a pinned host copy of it that each call queues after its work, the event
+// recorded after that copy, and whether such a copy is outstanding.
+struct NoAllocLink {
+    const SceneDev* scene;
+    int device;
+    uint32_t semantics;
+    bool fast_slabs;
+    uint32_t* error_word;
+    uint32_t* host_error;
+    cudaEvent_t* done;
+    bool* pending;
+};
+
 // Longest-first pixel order (order.cu): from the per-pixel costs of one
 // launch, the hand-out order of the next (tiles of 32 pixels by decreasing
 // summed cost).  Buffers: keys/vals/keys2/vals2 one entry per tile, `temp`

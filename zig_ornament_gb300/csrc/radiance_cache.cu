@@ -143,7 +143,11 @@ __device__ __forceinline__ uint32_t cta_setup(uint32_t* tmem_slot, uint64_t* mba
 }
 
 // After a timed-out wait: give the MMAs in flight one more bounded wait,
-// record the failure, then free the TMEM columns (on every path).
+// record the failure, then free the TMEM columns (on every path).  Freeing
+// while an MMA might still write them is only reached when both waits (3 s)
+// ran out; a CTA that exited holding its columns would instead leave them
+// allocated for every later CTA on that SM, whose tcgen05.alloc could then
+// wait forever, so the columns are always returned.
 __device__ __forceinline__ void cta_teardown(Sync& s, uint32_t tmem, uint32_t* status) {
     if (!s.ok) {
         tc::mbar_wait(s.mbar, s.phase, 1000000000ull);

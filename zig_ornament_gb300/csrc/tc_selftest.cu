@@ -57,7 +57,9 @@ tc_selftest_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ 
         tc::mma_commit(&mbar);
     }
     bool ok = tc::mbar_wait(&mbar, 0, 1000000000ull);
-    if (!ok) ok = tc::mbar_wait(&mbar, 0, 1000000000ull);   // in-flight MMAs: wait once more
+    // in-flight MMAs: wait once more; the columns are freed in any case (a
+    // CTA leaving them allocated could block later allocations on the SM)
+    if (!ok) ok = tc::mbar_wait(&mbar, 0, 1000000000ull);
     tc::fence_after_sync();
     if (ok) {
         for (uint32_t c = 0; c < N; c += 16) {
