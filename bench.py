@@ -14,10 +14,19 @@ the configuration's sample count) continuing the progressive render.
            1080p RGBA32F framebuffer comes back), timed by CUDA events.
   roofline algorithmic bytes per megakernel launch from exact work counters
            of one extra (untimed) step — node visits, leaf transforms, hit
-           shading gathers, per-sample buffer traffic — divided by the
-           average launch time, against the measured HBM copy bandwidth.
+           shading gathers, per-sample buffer traffic — over the average
+           launch time.  The L2-resident scenes are bound by the L1/TEX
+           pipeline and issue slots: `bound` "l1tex", against the nominal L1
+           load bandwidth, with the ncu figures of this build (SOL
+           percentages, active threads per warp) and the HBM share beside
+           it; the large scene is bound by HBM latency: `bound` "hbm",
+           DRAM traffic against the measured copy bandwidth.  ncu figures
+           come from the committed profiles/ summary of the same kernel
+           sources (null when the sources changed since that capture).
   cpu_baseline  the CPU restatement of the reference (oracle/oracle.cpp, all
-           host threads) on a bounded sample of the same workload.
+           host threads, -O3) on a bounded sample of the same workload, with
+           its measured speed relative to the reference's own kernels
+           (oracle/port_speed.json).
 
 `--impl reference` times the reference implementation of the path on the
 host cores (the CPU restatement, pinned bit-for-bit to the reference's own
@@ -27,12 +36,17 @@ Multi-GPU: one process per GPU (torchrun); every rank renders its own copy
 of the frame (replicas: pixels and samples are independent, no exchange);
 value = all ranks' samples / the slowest rank's time.
 
-The headline line also carries the same steps on the non-parity trees
-(`sah_tree`, `lbvh_tree`) and the time-to-relMSE block (plain megakernel
-against the cached renderers, two scenes at 640x360).  Other modes:
-`--workload spheres|large`, `--bvh sah|lbvh`, `--mode relmse` (the block
-alone), `--mode batch` (64 scenes in one graph-replayed launch against
-sequential launches), `--mode cached-frames [--batched]` (a profiling
+The headline line also carries: the same steps on the non-parity trees
+(`sah_tree`, `lbvh_tree`); `configs` — the sphere field (640x360, 64 spp),
+the large scene (3840x2160, 16 spp, depth 16) and the 64-scene batch (every
+scene's full sample count, one graph-replayed launch against one launch per
+scene), each with rays/s, roofline and CPU baseline; and `time_to_relmse` —
+plain tracing on the parity and SAH trees against the cached renderers, to
+relMSE 1e-3 against a 16k-sample FP64 oracle, on the radiance-cache
+configuration at 1920x1080 and a closed room at 640x360.  Other modes:
+`--workload spheres|large`, `--bvh sah|lbvh`, `--kernel wavefront`,
+`--mode relmse` (the block alone; `--workload large` for the large scene at
+960x540), `--mode batch`, `--mode cached-frames [--batched]` (a profiling
 workload of radiance-cache frames).
 """
 from __future__ import annotations
@@ -91,11 +105,13 @@ def parse():
     p.add_argument("--tune-cache", default=None, help="batch: autotuner JSON cache (default: none)")
     p.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE block")
     p.add_argument("--no-sah-line", action="store_true", help="skip the SAH-tree figure")
-    p.add_argument("--relmse-width", type=int, default=640)
-    p.add_argument("--relmse-height", type=int, default=360)
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the other configurations (sphere field, 64-scene batch, large scene)")
+    p.add_argument("--relmse-width", type=int, default=1920)
+    p.add_argument("--relmse-height", type=int, default=1080)
     p.add_argument("--relmse-target", type=float, default=1e-3)
     p.add_argument("--relmse-ref-spp", type=int, default=16384)
-    p.add_argument("--relmse-budget", type=float, default=8.0, help="GPU seconds per method at most")
+    p.add_argument("--relmse-budget", type=float, default=12.0, help="GPU seconds per method at most")
     p.add_argument("--frames", type=int, default=8, help="cached-frames: timed frames")
     p.add_argument("--batched", action="store_true",
                    help="cached-frames: the cached + batched configuration of the relMSE harness (8 sample "
@@ -148,7 +164,8 @@ def workload(args):
            "triangles": tris, "instances": len(scene.mesh_instances), "blas": len(scene.meshes),
            "tlas_nodes": int(len(bvh.tlas_nodes)), "blas_nodes": int(len(bvh.blas_nodes)),
            "kernel": ("plain megakernel (persistent, warp-synchronous, passes looped per pixel)"
-                      if args.kernel == "mega" else "persistent wavefront (logic + extend, compacted ray queue)"),
+                      if args.kernel == "mega" else "persistent wavefront (per-block path pools, ray and hit "
+                                                   "queues in shared memory, warps traverse or shade)"),
            "semantics": "HIP", "transcendentals": "portable (bit-exact with the CPU oracle)",
            "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
     return scene, bvh, cfg
@@ -257,18 +274,84 @@ def cpu_baseline(bvh, scene, args, seconds, threads=0):
     return value, nthreads, f"every {stride}th pixel of the frame ({pixels} pixels) x {spp} spp, {dt:.1f} s"
 
 
-def dram_traffic_per_launch():
-    """DRAM bytes (read + write) of one bench-size megakernel launch, from
-    the committed ncu summary (profiles/mega_kernel_1080p_32spp.md)."""
-    p = ROOT / "profiles" / "mega_kernel_1080p_32spp.md"
-    if p.exists():
-        for line in p.read_text().splitlines():
-            if line.strip().startswith("dram_bytes_per_launch:"):
-                try:
-                    return int(line.split(":", 1)[1].strip())
-                except ValueError:
-                    return None
-    return None
+def source_hash():
+    """Hash of the kernel sources and build flags (csrc/, include/, build.py):
+    identifies the build an ncu capture was taken of."""
+    import hashlib
+    h = hashlib.sha256()
+    files = (sorted((ROOT / "zig_ornament_gb300" / "csrc").glob("*")) + sorted((ROOT / "include").glob("*.h"))
+             + [ROOT / "zig_ornament_gb300" / "build.py"])
+    for f in files:
+        if f.is_file():
+            h.update(f.name.encode())
+            h.update(f.read_bytes())
+    return h.hexdigest()[:16]
+
+
+def profile_figures(name):
+    """(figures, source) of a committed ncu summary, profiles/<name>.md, whose
+    `figures:` line holds the counters bench.py quotes (DRAM bytes per node
+    visit, SOL percentages); figures is None unless that capture was taken
+    of the current kernel sources (source_hash)."""
+    p = ROOT / "profiles" / f"{name}.md"
+    if not p.exists():
+        return None, f"profiles/{name}.md absent"
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("figures:"):
+            try:
+                d = json.loads(line.split(":", 1)[1])
+            except ValueError:
+                return None, f"profiles/{name}.md: unreadable figures line"
+            if d.get("sources") != source_hash():
+                return None, f"profiles/{name}.md was captured from other kernel sources"
+            return d, f"profiles/{name}.md (ncu, this build)"
+    return None, f"profiles/{name}.md has no figures line"
+
+
+def l1_peak_gbs(clocks, device=0):
+    """Nominal L1 load bandwidth of the GPU: 128 bytes per clock per SM at
+    the maximum SM clock (not a measured figure)."""
+    import torch
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+    return sms * 128 * mhz * 1e6 / 1e9
+
+
+def roofline_block(bytes_per_launch, avg_launch_s, workload, clocks, profile_name, device=0, visits_per_launch=None):
+    """The roofline object of a megakernel workload.
+
+    L2-resident scenes (every workload but `large`): the kernel is bound by
+    the L1/TEX pipeline and issue slots (ncu: L1/TEX throughput and issue
+    activity near 60 %, DRAM below 1 %), so `achieved` (algorithmic bytes per
+    launch over the measured launch time) is set against the nominal L1 load
+    bandwidth, and the ncu figures of this build are quoted beside it.
+    The large scene (1.3 GB of nodes, L2 hit rate ~60 %) is bound by HBM
+    latency: `achieved` is the DRAM traffic of one launch over the launch
+    time, against the measured HBM copy bandwidth.  `traffic` = DRAM bytes
+    per node visit of the ncu capture of this build (a smaller launch of the
+    same scene) x this launch's node visits."""
+    peak_hbm, kind = measured_peaks()
+    algo = bytes_per_launch / avg_launch_s / 1e9
+    fig, src = profile_figures(profile_name) if profile_name else (None, "no profile")
+    traffic = None
+    if fig and "dram_bytes_per_visit" in fig and visits_per_launch:
+        traffic = fig["dram_bytes_per_visit"] * visits_per_launch
+    hbm = {"achieved": traffic / avg_launch_s / 1e9 if traffic else None, "peak": peak_hbm, "unit": "GB/s",
+           "peak_kind": f"{kind} HBM copy"}
+    hbm["frac"] = hbm["achieved"] / peak_hbm if hbm["achieved"] else None
+    if workload == "large":
+        out = {"bound": "hbm", "achieved": hbm["achieved"], "peak": peak_hbm, "unit": "GB/s", "frac": hbm["frac"],
+               "traffic": traffic, "peak_kind": f"{kind} HBM copy",
+               "algorithmic": {"achieved": algo, "unit": "GB/s",
+                               "note": "node and shading bytes the algorithm reads, L1/L2-served ones included"}}
+    else:
+        l1 = l1_peak_gbs(clocks, device)
+        out = {"bound": "l1tex", "achieved": algo, "peak": l1, "unit": "GB/s", "frac": algo / l1,
+               "traffic": traffic, "peak_kind": "nominal L1 load bandwidth (128 B/clk/SM x SMs x max SM clock)",
+               "hbm": hbm}
+    out["ncu"] = ({k: fig[k] for k in fig if k not in ("sources",)} if fig else None)
+    out["ncu_source"] = src
+    return out
 
 
 def run_reference(args):
@@ -395,12 +478,9 @@ def run_ours(args):
         if dist:
             dist.destroy_process_group()
         return
-    peak, peak_kind = measured_peaks()
     avg_launch_s = (sum(step_ms) / 1e3) / max(launches, 1)
     bytes_per_launch = algorithmic_bytes(counters) / max(launches_per_step, 1)
-    achieved = bytes_per_launch / avg_launch_s / 1e9
-    traffic = (dram_traffic_per_launch()
-               if (args.kernel == "mega" and args.spp >= 32 and metric_name(args) == METRIC) else None)
+    clk = clocks.summary()
     line = {
         "metric": metric_name(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -411,17 +491,13 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "rays_per_s": counters["rays"] / samples_step * value * 1e6,
         "work_per_step": counters,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} HBM copy",
-                     "note": ("algorithmic bytes are served mostly by L1/L2 (the scene is L2-resident); "
-                              "the limiter is L1/TEX throughput and issue slots (profiles/)")
-                             if args.workload != "large" else
-                             ("1.3 GB of BVH nodes do not fit the 129 MB L2: node fetches go to HBM; "
-                              f"latency-bound at {counters['visits'] / max(counters['rays'], 1):.0f} node "
-                              "visits per ray (profiles/)")},
-        "clocks": clocks.summary(),
+        "roofline": roofline_block(bytes_per_launch, avg_launch_s, args.workload, clk,
+                                   PROFILE_OF_WORKLOAD.get(args.workload if args.kernel == "mega" else "wavefront"),
+                                   local, counters["visits"] / max(launches_per_step, 1)),
+        "clocks": clk,
     }
-    if args.kernel == "mega" and args.bvh == "reference" and not args.no_sah_line:
+    headline = args.kernel == "mega" and args.bvh == "reference" and metric_name(args) == METRIC
+    if headline and not args.no_sah_line:
         # the same steps on the non-parity trees, for reference
         for alt in ("sah", "lbvh"):
             key = alt + "_tree"
@@ -429,39 +505,141 @@ def run_ours(args):
                 t_alt = time.perf_counter()
                 alt_bvh = ornament.Bvh(scene, builder=alt)
                 t_alt = time.perf_counter() - t_alt
-                rs = ornament.Renderer(alt_bvh, device=local)
-                rs.set_resolution(args.width, args.height)
-                rs.set_state(st)
-                rs.set_camera(scene.camera.to_struct())
-                for _ in range(args.warmup):
-                    rs.render()
-                sms = []
-                for _ in range(args.steps):
-                    rs.render()
-                    sms.append(rs.last_render_ms())
-                line[key] = {"value": samples_step / (sum(sms) / len(sms) / 1e3) / 1e6, "unit": UNIT,
-                             "bvh_build_s": round(t_alt, 3),
+                m = measure_megakernel(alt_bvh, scene, args.width, args.height, args.spp, args.depth,
+                                       args.steps, args.warmup, local, flush)
+                line[key] = {"value": m["value"], "unit": UNIT, "bvh_build_s": round(t_alt, 3),
                              "note": f"same steps on the {TREE_DESC[alt]} tree: images equal to the "
                                      "reference's in expectation only"}
-                rs.close()
             except Exception as exc:
                 line[key] = {"error": f"{type(exc).__name__}: {exc}"}
-    if not args.no_relmse and args.kernel == "mega" and args.workload == "instanced" and args.bvh == "reference":
-        try:
-            line["time_to_relmse"] = relmse_block(args)
-        except Exception as exc:   # the throughput line stands on its own
-            line["time_to_relmse"] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.no_cpu_baseline:
         v, cores, desc = cpu_baseline(bvh, scene, args, args.cpu_seconds)
         v1, _, desc1 = cpu_baseline(bvh, scene, args, 4.0, threads=1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": desc + "; CPU restatement of the reference (bit-exact with its own "
                                           "kernels compiled for the host)",
-                                "single_thread": {"value": v1, "sample": desc1}}
+                                "single_thread": {"value": v1, "sample": desc1}, **port_speed_note()}
+    if headline and not args.no_configs:
+        line["configs"] = other_configs(args, local, flush)
+    if headline and not args.no_relmse:
+        try:
+            line["time_to_relmse"] = relmse_block(args)
+        except Exception as exc:   # the throughput line stands on its own
+            line["time_to_relmse"] = {"error": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line), flush=True)
     r.close()
     if dist:
         dist.destroy_process_group()
+
+
+# Committed ncu summary (profiles/<name>.md) of each workload's render kernel.
+PROFILE_OF_WORKLOAD = {"instanced": "mega_kernel_1080p_32spp", "spheres": "mega_kernel_spheres_640x360",
+                       "large": "mega_kernel_large_960x540", "wavefront": "wave_kernel_1080p"}
+
+
+def port_speed_note():
+    """The restatement's flags and its measured speed relative to the
+    reference's own kernels (oracle/port_speed.py, run where the reference
+    sources are; the GPU host has no copy of them)."""
+    from oracle import build_oracle as bo
+    note = {"flags": " ".join(f for f in bo.FLAGS if f.startswith(("-O", "-ff", "-fno", "-fopenmp")))}
+    p = ROOT / "oracle" / "port_speed.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        note["port_over_reference"] = {
+            "restatement_over_reference": d.get("restatement_over_reference"),
+            "restatement_over_reference_same_math": d.get("restatement_over_reference_same_math"),
+            "measured_on": d.get("host"), "workload": d.get("workload"), "source": "oracle/port_speed.json"}
+    return note
+
+
+def measure_megakernel(bvh, scene, w, h, spp, depth, steps, warmup, local, flush, counters=False):
+    """Device time of `steps` renders of `spp` passes (L2 flushed between
+    them); returns Msamples/s, ms per step, launches per step and, with
+    `counters`, the exact work of one more (untimed) render."""
+    import torch
+    from zig_ornament_gb300 import _lib, ornament
+    r = ornament.Renderer(bvh, device=local)
+    r.set_resolution(w, h)
+    st = _lib.State()
+    st.depth, st.flip_y, st.inverted_gamma, st.iterations = depth, 0, 1.0, spp
+    st.ray_cast_epsilon, st.semantics, st.spp_per_launch = 0.001, 0, 0
+    st.kernel = _lib.KERNEL_MEGA
+    r.set_state(st)
+    r.set_camera(scene.camera.to_struct())
+    stream = torch.cuda.ExternalStream(r.stream(), device=torch.device("cuda", local))
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(warmup):
+        r.render()
+        flush_l2()
+    r.synchronize()
+    l0 = r.launch_count()
+    ms = []
+    for _ in range(steps):
+        r.render()
+        ms.append(r.last_render_ms())
+        flush_l2()
+    r.synchronize()
+    launches = (r.launch_count() - l0) / steps
+    out = {"value": w * h * spp / (float(np.mean(ms)) / 1e3) / 1e6, "ms_per_step": float(np.mean(ms)),
+           "launches_per_step": launches}
+    if counters:
+        r.enable_counters(True)
+        r.render()
+        out["counters"] = r.counters()
+        r.enable_counters(False)
+    r.close()
+    return out
+
+
+def other_configs(args, local, flush):
+    """The other configurations, compactly: the sphere field (640x360,
+    64 spp, depth 10), the 64-scene batch (one persistent launch from a CUDA
+    graph against one launch per scene) and the large scene (4096 instances,
+    ~10M triangles, 3840x2160, 16 spp, depth 16), each with its rays/s,
+    roofline and the CPU restatement on a bounded sample."""
+    import copy
+    out = {}
+    for key, wl, steps, warmup, cpu_s in (("cfg0_spheres", "spheres", 3, 3, 3.0), ("cfg4_large", "large", 2, 1, 4.0)):
+        t0 = time.time()
+        try:
+            a = copy.copy(args)
+            a.workload, a.width, a.height, a.spp, a.depth = wl, None, None, None, None
+            a = apply_workload_defaults(a)
+            scene, bvh, cfg = workload(a)
+            m = measure_megakernel(bvh, scene, a.width, a.height, a.spp, a.depth, steps, warmup, local, flush,
+                                   counters=True)
+            c = m["counters"]
+            launch_s = m["ms_per_step"] / 1e3 / max(m["launches_per_step"], 1)
+            bpl = algorithmic_bytes(c) / max(m["launches_per_step"], 1)
+            cpu_v, cores, desc = cpu_baseline(bvh, scene, a, cpu_s)
+            out[key] = {"metric": metric_name(a), "value": m["value"], "unit": UNIT,
+                        "ms_per_step": m["ms_per_step"], "steps": steps, "warmup": warmup,
+                        "rays_per_s": c["rays"] / (a.width * a.height * a.spp) * m["value"] * 1e6,
+                        "visits_per_ray": c["visits"] / max(c["rays"], 1),
+                        "roofline": roofline_block(bpl, launch_s, wl, None, PROFILE_OF_WORKLOAD[wl], local,
+                                                   c["visits"] / max(m["launches_per_step"], 1)),
+                        "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
+                                         "sample": desc},
+                        "ratio_vs_cpu": m["value"] / cpu_v,
+                        "config": {k: cfg[k] for k in ("workload", "resolution", "spp_per_step", "depth",
+                                                        "triangles", "instances", "blas_nodes", "bvh_build_s")},
+                        "wall_s": round(time.time() - t0, 1)}
+        except Exception as exc:
+            out[key] = {"error": f"{type(exc).__name__}: {exc}"}
+    t0 = time.time()
+    try:
+        b = copy.copy(args)
+        b.steps, b.warmup, b.depth = 1, 1, 8
+        out["cfg2_batch"] = batch_measure(b, divisor=1)
+        out["cfg2_batch"]["wall_s"] = round(time.time() - t0, 1)
+    except Exception as exc:
+        out["cfg2_batch"] = {"error": f"{type(exc).__name__}: {exc}"}
+    return out
 
 
 # ---- time to relMSE ------------------------------------------------------------------
@@ -469,6 +647,8 @@ def relmse_scene(name, w, h):
     from zig_ornament_gb300 import scenes
     if name == "closed-room":
         return scenes.cornell_box_scene(w, h)
+    if name == "large":
+        return scenes.large_scene(w, h)
     # the radiance-cache configuration: the 1080p instanced-mesh scene with
     # three emissive quads (rendered at the harness resolution)
     return scenes.instanced_meshes_scene(w, h, n_lights=3)
@@ -493,20 +673,24 @@ def crossing_time(curve, target):
 def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=None, warmup=64, methods=None,
                    ref=None, streams=8, batched_warmup_spp=16, batched_sobol=True, batched_cfg=None):
     """GPU time each renderer needs to bring the relMSE against an FP64
-    `ref_spp`-sample oracle (orn_render_f64) down to `target`: plain
-    megakernel tracing, the cached renderer without the network (every pixel
-    traces its full path with light sampling: unbiased), the cached
-    renderer as configured (lr 1e-3, 64 warm-up training frames counted),
-    and the cached renderer tuned: on the SAH tree (a non-parity tree, like
-    the cached renderer itself), Adam lr 3e-3, 32 warm-up frames; and
-    cached + batched: on the SAH tree, `streams` sample streams per pixel
-    batched into each frame's launch (orn_state.spp_per_launch), the Sobol
-    sampler, training slots for 1/8 of the samples at lr 5e-3, a 16-sample
-    warm-up.  Progressive rendering
-    in growing chunks; relMSE (orn_relmse, FP64 on the GPU) is read between
-    chunks outside the timed renders; the crossing is interpolated
-    log-linearly between the two chunks around it, or extrapolated as
-    relMSE ~ 1/time past the budget (crossing_time)."""
+    `ref_spp`-sample oracle (orn_render_f64 with the plain megakernel on the
+    parity tree) down to `target`:
+      plain           the plain megakernel on the parity tree (bvh.zig's rules),
+      plain_sah       the plain megakernel on the binned-SAH tree, the tree of
+                      cached_tuned and cached_batched,
+      light_sampling  the cached renderer without the network (every pixel
+                      traces its full path with light sampling: unbiased),
+      cached          the cached renderer as configured (lr 1e-3, 64 warm-up
+                      training frames counted), parity tree,
+      cached_tuned    Adam lr 3e-3, 32 warm-up frames, SAH tree,
+      cached_batched  `streams` sample streams per pixel batched into each
+                      frame's launch (orn_state.spp_per_launch), the Sobol
+                      sampler, training slots for 1/8 of the samples at lr
+                      5e-3, a 16-sample warm-up, SAH tree.
+    Progressive rendering in growing chunks; relMSE (orn_relmse, FP64 on the
+    GPU) is read between chunks outside the timed renders; the crossing is
+    interpolated log-linearly between the two chunks around it, or
+    extrapolated as relMSE ~ 1/time past the budget (crossing_time)."""
     from zig_ornament_gb300 import _lib, ornament
 
     scene = relmse_scene(name, w, h)
@@ -529,19 +713,21 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         ref = rr.render_f64(ref_spp)
         rr.close()
     ref_s = time.time() - t0
-    out = {"resolution": f"{w}x{h}", "reference_spp": ref_spp, "reference_seconds": round(ref_s, 1)}
-    for method in (methods or ("plain", "light_sampling", "cached", "cached_tuned", "cached_batched")):
-        kernel = _lib.KERNEL_MEGA if method == "plain" else _lib.KERNEL_CACHED
+    out = {"resolution": f"{w}x{h}", "depth": depth, "reference_spp": ref_spp, "reference_seconds": round(ref_s, 1),
+           "reference": "plain megakernel, parity tree, FP64 accumulation"}
+    on_sah = ("plain_sah", "cached_tuned", "cached_batched")
+    for method in (methods or ("plain", "plain_sah", "light_sampling", "cached", "cached_tuned", "cached_batched")):
+        kernel = _lib.KERNEL_MEGA if method in ("plain", "plain_sah") else _lib.KERNEL_CACHED
         tuned = method in ("cached_tuned", "cached_batched")
-        if tuned and bvh_sah is None:
+        if method in on_sah and bvh_sah is None:
             bvh_sah = ornament.Bvh(scene, row_major_transforms=True, builder="sah")
-        r, st = renderer(kernel, bvh_sah if tuned else None)
+        r, st = renderer(kernel, bvh_sah if method in on_sah else None)
         if method == "cached_batched":
             st.spp_per_launch = streams
             st.sampler = _lib.SAMPLER_SOBOL if batched_sobol else _lib.SAMPLER_PCG
         cache = None
         t = 0.0
-        if method != "plain":
+        if kernel == _lib.KERNEL_CACHED:
             if method == "light_sampling":
                 cfg = {"train_shift": 0, "steps_per_frame": 0}
             elif method == "cached_batched":
@@ -580,26 +766,46 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         tt, reached = crossing_time(curve, target)
         out[method] = {"seconds": round(tt, 4), "reached": reached,
                        "samples_per_pixel": n, "final_relmse": curve[-1][2],
+                       "tree": "SAH" if method in on_sah else "parity",
                        "curve": [[round(a, 4), b, float("%.4g" % c)] for a, b, c in curve]}
         r.close()
         if cache is not None:
             cache.close()
     if "cached_batched" in out:
         out["cached_batched"]["streams"] = streams
-    for m in ("cached", "cached_tuned", "cached_batched", "light_sampling"):
+    for m in ("plain_sah", "cached", "cached_tuned", "cached_batched", "light_sampling"):
         if m in out and "plain" in out:
             out[f"speedup_{m}_vs_plain"] = round(out["plain"]["seconds"] / out[m]["seconds"], 3)
+    for m in ("cached_tuned", "cached_batched"):
+        if m in out and "plain_sah" in out:
+            out[f"speedup_{m}_vs_plain_same_tree"] = round(out["plain_sah"]["seconds"] / out[m]["seconds"], 3)
+    if "speedup_cached_batched_vs_plain_same_tree" in out:
+        v = out["speedup_cached_batched_vs_plain_same_tree"]
+        out["target_5x_same_tree"] = ("met" if v >= 5.0 else f"not met ({v}x against the plain megakernel on "
+                                      "the same SAH tree)")
     out["_ref"] = ref
     return out
 
 
 def relmse_block(args):
+    """The radiance-cache configuration's scene at its own resolution
+    (--relmse-width x --relmse-height, default 1920x1080), and the closed
+    room (a scene this project adds: long multi-bounce paths) at 640x360.
+    With --workload large: the large scene (depth 16) at 960x540 instead —
+    its 16k-sample FP64 oracle at 3840x2160 would take about an hour of GPU
+    time at the plain megakernel's rate."""
     res = {"target": args.relmse_target, "metric": "GPU seconds to relMSE <= target vs FP64 oracle",
            "scenes": {}}
-    for name in ("instanced", "closed-room"):
-        res["scenes"][name] = time_to_relmse(name, args.relmse_width, args.relmse_height, args.relmse_target,
-                                             args.relmse_ref_spp, args.relmse_budget)
+    if args.workload == "large":
+        todo = (("large", 960, 540, 16),)
+    else:
+        todo = (("instanced", args.relmse_width, args.relmse_height, 8), ("closed-room", 640, 360, 8))
+    for name, w, h, depth in todo:
+        t0 = time.time()
+        res["scenes"][name] = time_to_relmse(name, w, h, args.relmse_target, args.relmse_ref_spp, args.relmse_budget,
+                                             depth=depth)
         res["scenes"][name].pop("_ref")
+        res["scenes"][name]["wall_s"] = round(time.time() - t0, 1)
     return res
 
 
@@ -640,26 +846,27 @@ def run_cached_frames(args):
     cache.close()
 
 
-def run_batch(args):
+def batch_measure(args, divisor=None):
     """The batched-rendering configuration: --batch-scenes independent
     instanced-mesh scenes (total BLAS triangles log-uniform 1k-2M, 1-1024
     instances, resolutions from {256^2, 640x360, 1280x720, 1920x1080}, 16-256
     samples per pixel, depth 8), one frame = spp/divisor passes of every
-    scene.  Sequential: each context's own orn_render (one megakernel launch
-    per scene), summed device times; batched: orn_batch_render (one
-    persistent launch replayed from a CUDA graph, launch shape from the
-    autotuner), device time per frame."""
+    scene (divisor 1: every scene's full sample count).  Sequential: each
+    context's own orn_render (one megakernel launch per scene), summed device
+    times; batched: orn_batch_render (one persistent launch replayed from a
+    CUDA graph, launch shape from the autotuner), device time per frame."""
     from zig_ornament_gb300 import ornament, scenes
+    divisor = divisor or args.batch_spp_divisor
     t0 = time.time()
     work = scenes.batch_scenes(count=args.batch_scenes, seed=2)
-    ctxs, samples, nodes = [], 0, 0
+    ctxs, samples, nodes, rays = [], 0, 0, 0
     for sc, w, h, spp in work:
         bvh = ornament.Bvh(sc, row_major_transforms=True)
         r = ornament.Renderer(bvh, 0)
         r.set_resolution(w, h)
         st = ornament.State()
         st.depth = args.depth
-        st.iterations = max(1, -(-spp // args.batch_spp_divisor))
+        st.iterations = max(1, -(-spp // divisor))
         r.set_state(st.to_struct())
         r.set_camera(sc.camera.to_struct())
         ctxs.append(r)
@@ -680,6 +887,12 @@ def run_batch(args):
             r.render()
             total += r.last_render_ms()
         seq_ms.append(total)
+    # the work of one frame (exact counters, untimed)
+    for r in ctxs:
+        r.enable_counters(True)
+        r.render()
+        rays += r.counters()["rays"]
+        r.enable_counters(False)
     batch = ornament.Batch(ctxs)
     t1 = time.time()
     cfg = batch.tune(args.tune_cache)
@@ -694,22 +907,32 @@ def run_batch(args):
             bat_ms.append(batch.last_render_ms())
     seq = samples / (np.mean(seq_ms) / 1e3) / 1e6
     bat = samples / (np.mean(bat_ms) / 1e3) / 1e6
-    line = {"mode": "batch", "metric": "Msamples/s, batched scenes", "unit": "Msamples/s",
-            "batched": bat, "sequential": seq, "speedup": bat / seq,
+    line = {"metric": "Msamples/s, batched scenes", "unit": "Msamples/s",
+            "value": bat, "sequential": seq, "speedup": bat / seq,
+            "rays_per_s": rays / samples * bat * 1e6,
             "ms_per_frame": {"batched": float(np.mean(bat_ms)), "sequential": float(np.mean(seq_ms))},
             "steps": args.steps, "warmup": args.warmup,
             "config": {"workload": f"{len(ctxs)} instanced-mesh scenes, total BLAS triangles log-uniform "
                                    "1k-2M, 1-1024 instances, resolutions 256^2..1920x1080, 16-256 spp, depth "
-                                   f"{args.depth}; one frame = spp/{args.batch_spp_divisor} passes per scene",
+                                   f"{args.depth}; one frame = "
+                                   + ("every scene's full sample count" if divisor == 1 else
+                                      f"spp/{divisor} passes per scene"),
                        "pixels": int(sum(w * h for _, w, h, _ in work)), "samples_per_frame": int(samples),
                        "blas_nodes": int(nodes), "launch": cfg, "tune_seconds": round(tune_s, 2),
                        "setup_seconds": round(setup_s, 1)},
             "gpu_launches_per_frame": {"batched": 1, "sequential": len(ctxs)},
             "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
     batch.close()
     for r in ctxs:
         r.close()
+    return line
+
+
+def run_batch(args):
+    line = batch_measure(args)
+    line["mode"] = "batch"
+    line["batched"] = line["value"]
+    print(json.dumps(line), flush=True)
 
 
 def main():

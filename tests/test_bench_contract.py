@@ -42,3 +42,35 @@ def test_relmse_crossing_time():
     # never reached: extrapolated as relMSE ~ 1/time
     t, reached = bench.crossing_time([(1.0, 16, 4e-3), (2.0, 32, 2e-3)], 1e-3)
     assert not reached and abs(t - 4.0) < 1e-9
+
+
+def test_profile_figures_only_for_the_current_build(tmp_path, monkeypatch):
+    """bench.py quotes ncu counters from a committed profile summary only
+    when that capture was taken of the current kernel sources."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    h = bench.source_hash()
+    assert h == bench.source_hash() and len(h) == 16
+    prof = tmp_path / "profiles"
+    prof.mkdir()
+    fig = {"sources": h, "dram_bytes_per_visit": 1.5, "l1tex_pct": 60.0}
+    (prof / "k_now.md").write_text("# k\n\nfigures: " + json.dumps(fig) + "\n")
+    (prof / "k_old.md").write_text("figures: " + json.dumps(dict(fig, sources="0" * 16)) + "\n")
+    (prof / "k_none.md").write_text("# no figures\n")
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    monkeypatch.setattr(bench, "source_hash", lambda: h)
+    d, src = bench.profile_figures("k_now")
+    assert d["dram_bytes_per_visit"] == 1.5 and "this build" in src
+    assert bench.profile_figures("k_old")[0] is None
+    assert bench.profile_figures("k_none")[0] is None
+    assert bench.profile_figures("k_absent")[0] is None
+
+
+def test_port_speed_record():
+    """The restatement's speed against the reference's own kernels (same
+    flags, same cores), measured where the reference sources are."""
+    d = json.loads((ROOT / "oracle" / "port_speed.json").read_text())
+    assert d["accumulation_bit_identical"] is True
+    assert "-O3" in d["flags"] and "-ffp-contract=off" in d["flags"]
+    for k in ("all_threads", "one_thread"):
+        assert d["restatement_over_reference"][k] > 0
