@@ -161,10 +161,16 @@ enum orn_semantics { ORN_SEMANTICS_HIP = 0, ORN_SEMANTICS_WGSL = 1 };
 
 /* Kernel variant used by orn_render. */
 enum orn_kernel {
-    ORN_KERNEL_MEGA = 0,      /* one thread per pixel, samples looped in-thread */
-    ORN_KERNEL_WAVEFRONT = 1, /* persistent path pool + compacted ray queues   */
-    ORN_KERNEL_CACHED = 2     /* megakernel + learned radiance cache (orn_attach_cache);
-                                 biased, not bit-exact with the reference     */
+    ORN_KERNEL_MEGA = 0,        /* persistent warp-synchronous megakernel, a pixel's
+                                   samples looped in one lane */
+    ORN_KERNEL_WAVEFRONT = 1,   /* persistent wavefront: per-block path pools, ray and
+                                   hit queues in shared memory, warps that traverse
+                                   or shade (same bits as MEGA) */
+    ORN_KERNEL_CACHED = 2,      /* learned radiance cache (orn_attach_cache) on the
+                                   persistent wavefront; biased, not bit-exact with
+                                   the reference */
+    ORN_KERNEL_CACHED_MEGA = 3  /* the same cached renderer on the megakernel (the
+                                   same estimator, path for path) */
 };
 
 /* State, src/state.zig:3-23 (resolution set by orn_set_resolution). */

@@ -300,3 +300,34 @@ def test_sobol_sampler_is_unbiased():
         r.close()
         cache.close()
     assert errs[_lib.SAMPLER_SOBOL] < errs[_lib.SAMPLER_PCG]
+
+
+@pytest.mark.parametrize("sampler", [_lib.SAMPLER_PCG, _lib.SAMPLER_SOBOL], ids=["pcg", "sobol"])
+@pytest.mark.parametrize("semantics", [_lib.SEMANTICS_HIP, _lib.SEMANTICS_WGSL], ids=["hip", "wgsl"])
+def test_cached_wavefront_matches_cached_megakernel(sampler, semantics):
+    """The cached renderer on the persistent wavefront (KERNEL_CACHED) runs
+    the cached megakernel's path logic (KERNEL_CACHED_MEGA) operation for
+    operation: with the network's part off (every path a training path,
+    train_shift 0, no training steps) and one sample stream, both give the
+    same accumulation and RNG states bit for bit over several frames —
+    light sampling, shadow rays, cache-vertex records and all."""
+    w, h = 160, 96
+    scene = _cache_scene(w, h)
+    out = {}
+    for kernel in (_lib.KERNEL_CACHED_MEGA, _lib.KERNEL_CACHED):
+        r, st = _renderer(scene, w, h, kernel)
+        st.sampler = sampler
+        st.semantics = semantics
+        cache = ornament.RadianceCache(seed=1, train_shift=0, steps_per_frame=0)
+        r.attach_cache(cache)
+        _run_for(r, st, scene, 6)
+        acc, rng, ci = r.progress()
+        out[kernel] = (np.ascontiguousarray(acc).view(np.uint32).copy(), rng.copy(), ci)
+        r.synchronize()
+        r.attach_cache(None)
+        r.close()
+        cache.close()
+    a, b = out[_lib.KERNEL_CACHED_MEGA], out[_lib.KERNEL_CACHED]
+    assert a[2] == b[2] == 6.0
+    assert np.array_equal(a[1], b[1])
+    assert np.array_equal(a[0], b[0])

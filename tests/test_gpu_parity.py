@@ -368,7 +368,8 @@ def test_sah_tree_renders_like_the_oracle(oracle, kernel):
     r.close()
 
 
-@pytest.mark.parametrize("kernel", [_lib.KERNEL_MEGA, _lib.KERNEL_CACHED], ids=["mega", "cached"])
+@pytest.mark.parametrize("kernel", [_lib.KERNEL_MEGA, _lib.KERNEL_WAVEFRONT, _lib.KERNEL_CACHED],
+                         ids=["mega", "wavefront", "cached"])
 def test_pixel_order_does_not_change_results(kernel):
     """Longest-first hand-out (orn_state.pixel_order = COST, the default)
     against raster order over several launches: the same bits."""

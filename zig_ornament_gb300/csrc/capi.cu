@@ -72,12 +72,6 @@ struct orn_context {
     mutable uint32_t* na_host_error = nullptr;
     mutable cudaEvent_t na_done = nullptr;
     mutable bool na_pending = false;
-    // wavefront path pool (allocated on first use)
-    uint32_t wf_slots = 0;
-    std::vector<void*> wf_allocs;
-    orn::WaveLaunch wf{};
-    uint32_t* wf_host_stat = nullptr;     // pinned ring of [count, pending] pairs
-    cudaEvent_t wf_events[16] = {};
     unsigned long long* d_counters = nullptr;
     bool counters_enabled = false;
     bool rendered = false;
@@ -435,6 +429,7 @@ int sync_and_check(orn_context* ctx) {
         if (err & orn::ERR_STACK)
             return fail(ctx, ORN_ERR_STACK_OVERFLOW, "a ray needed more than 64 traversal stack entries");
         if (err & orn::ERR_MMA) return fail(ctx, ORN_ERR_TIMEOUT, "a radiance-cache tensor-core wait timed out");
+        if (err & orn::ERR_WAIT) return fail(ctx, ORN_ERR_TIMEOUT, "a wavefront queue wait timed out");
         return fail(ctx, ORN_ERR_TIMEOUT, "a ray exceeded the per-ray node-visit limit");
     }
     return ORN_OK;
@@ -477,91 +472,9 @@ bool render_fast_slabs(const orn_context* ctx) {
     return 4.0 * ctx->max_inverse_entry * (s + 1.0) < 1e29;
 }
 
-constexpr int kWfRing = 16;
-constexpr int kWfLag = 6;
-
-// Allocates the wavefront path pool: min(pixels, 2^20) slots of structure-of-
-// arrays path state (about 120 bytes each) plus the ray queue.
-int ensure_wavefront(orn_context* ctx) {
-    const uint32_t pixels = ctx->width * ctx->height;
-    uint32_t want = std::min<uint32_t>(pixels, 1u << 20);
-    want = (want + 255) / 256 * 256;
-    if (ctx->wf_slots >= want) return ORN_OK;
-    for (void* p : ctx->wf_allocs) cudaFree(p);
-    ctx->wf_allocs.clear();
-    ctx->wf_slots = 0;
-    auto alloc = [&](size_t bytes, void** out) -> int {
-        ORN_CUDA(ctx, cudaMalloc(out, bytes));
-        ctx->wf_allocs.push_back(*out);
-        return ORN_OK;
-    };
-    orn::WaveLaunch& w = ctx->wf;
-    int st;
-    if ((st = alloc(4 * sizeof(uint32_t), (void**)&w.pixel_counter))) return st;
-    if ((st = alloc(16 * sizeof(uint32_t), (void**)&w.qstat))) return st;
-    if ((st = alloc((size_t)want * 4, (void**)&w.queue))) return st;
-    if ((st = alloc((size_t)want * 4, (void**)&w.mode))) return st;
-    if ((st = alloc((size_t)want * 4, (void**)&w.pixel))) return st;
-    if ((st = alloc((size_t)want * 8, (void**)&w.kb))) return st;
-    if ((st = alloc((size_t)want * 4, (void**)&w.rng_state))) return st;
-    if ((st = alloc((size_t)want * 16, (void**)&w.accum))) return st;
-    if ((st = alloc((size_t)want * 16, (void**)&w.color))) return st;
-    if ((st = alloc((size_t)want * 16, (void**)&w.ro))) return st;
-    if ((st = alloc((size_t)want * 16, (void**)&w.rd))) return st;
-    if ((st = alloc((size_t)want * 32, (void**)&w.hit))) return st;
-    if (!ctx->wf_host_stat) {
-        ORN_CUDA(ctx, cudaMallocHost(&ctx->wf_host_stat, kWfRing * 2 * sizeof(uint32_t)));
-        for (int i = 0; i < kWfRing; ++i)
-            ORN_CUDA(ctx, cudaEventCreateWithFlags(&ctx->wf_events[i], cudaEventDisableTiming));
-    }
-    ctx->wf_slots = want;
-    return ORN_OK;
-}
-
-// One sweep of the wavefront over every pixel: `spp` passes starting at
-// current_iteration = cp.current_iteration.  Iterations (logic, readback of
-// the queue length, extend) are issued ahead of the GPU; the loop stops once
-// an iteration kWfLag back produced no ray and left no slot waiting.
-int render_wavefront_sweep(orn_context* ctx, const orn_constant_params& cp, uint32_t spp, bool do_post) {
-    orn::WaveLaunch& w = ctx->wf;
-    w.scene = ctx->scene;
-    w.cp = cp;
-    w.spp = spp;
-    w.do_post = do_post ? 1u : 0u;
-    w.pixel_count = ctx->width * ctx->height;
-    w.slots = ctx->wf_slots;
-    w.acc = ctx->acc;
-    w.fb = ctx->fb;
-    w.rng = ctx->rng;
-    w.error = ctx->d_error;
-    w.counters = ctx->d_counters;
-    w.fetch_threshold = orn::kFetchThreshold;
-    ORN_CUDA(ctx, cudaMemsetAsync(w.mode, 0, (size_t)w.slots * 4, ctx->stream));
-    ORN_CUDA(ctx, cudaMemsetAsync(w.pixel_counter, 0, 4 * sizeof(uint32_t), ctx->stream));
-    ORN_CUDA(ctx, cudaMemsetAsync(w.qstat, 0, 16 * sizeof(uint32_t), ctx->stream));
-    const int sem = (int)ctx->state.semantics;
-    const bool fast = render_fast_slabs(ctx);
-    // Upper bound on iterations: every ray of every sample of every pixel
-    // (protects against a logic error turning into an endless host loop).
-    const uint64_t max_iter = (uint64_t)spp * (ctx->state.depth + 1) *
-                                  ((w.pixel_count + w.slots - 1) / w.slots) + 64;
-    for (uint64_t it = 0;; ++it) {
-        if (it >= (uint64_t)kWfLag) {
-            const int r = (int)((it - kWfLag) % kWfRing);
-            ORN_CUDA(ctx, cudaEventSynchronize(ctx->wf_events[r]));
-            if (ctx->wf_host_stat[2 * r] == 0 && ctx->wf_host_stat[2 * r + 1] == 0) break;
-        }
-        if (it > max_iter) return fail(ctx, ORN_ERR_TIMEOUT, "wavefront did not drain");
-        const uint32_t iter = (uint32_t)it;
-        ORN_CUDA(ctx, orn::launch_wf_logic(w, iter, sem, orn::MATH_PORTABLE, ctx->counters_enabled, ctx->stream));
-        const int r = (int)(it % kWfRing);
-        ORN_CUDA(ctx, cudaMemcpyAsync(ctx->wf_host_stat + 2 * r, w.qstat + 4 * (iter & 3), 2 * sizeof(uint32_t),
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-        ORN_CUDA(ctx, cudaEventRecord(ctx->wf_events[r], ctx->stream));
-        ORN_CUDA(ctx, orn::launch_wf_extend(w, iter, ctx->counters_enabled, fast, ctx->stream));
-        ctx->launches += 2;
-    }
-    return ORN_OK;
+// The cached renderer (on the wavefront or the megakernel).
+bool is_cached(const orn_context* ctx) {
+    return ctx->state.kernel == ORN_KERNEL_CACHED || ctx->state.kernel == ORN_KERNEL_CACHED_MEGA;
 }
 
 // Query queue and training slots of the cached renderer, sized for the
@@ -656,7 +569,10 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->cq_count, 0, 4, ctx->stream));
         // slots no training path writes this frame read as "no target" (NaN)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->ct_target, 0xFF, (size_t)ctx->cq_slots * 12, ctx->stream));
-        ORN_CUDA(ctx, orn::launch_mega_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
+        if (ctx->state.kernel == ORN_KERNEL_CACHED_MEGA)
+            ORN_CUDA(ctx, orn::launch_mega_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
+        else
+            ORN_CUDA(ctx, orn::launch_wave_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
         ctx->launches++;
         int st = orn::cache_apply_queries(c, ctx->cq_count, n * streams, ctx->cq_in, ctx->cq_pixel, ctx->cq_thr, ctx->acc,
                                           ctx->d_error, ctx->stream);
@@ -958,10 +874,6 @@ int orn_destroy(orn_context* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_target(ctx);
     for (void* p : ctx->scene_allocs) cudaFree(p);
-    for (void* p : ctx->wf_allocs) cudaFree(p);
-    if (ctx->wf_host_stat) cudaFreeHost(ctx->wf_host_stat);
-    for (cudaEvent_t e : ctx->wf_events)
-        if (e) cudaEventDestroy(e);
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_work) cudaFree(ctx->d_work);
     if (ctx->na_host_error) cudaFreeHost(ctx->na_host_error);
@@ -977,7 +889,7 @@ int orn_destroy(orn_context* ctx) {
 
 int orn_set_state(orn_context* ctx, const orn_state* s) {
     if (!ctx || !s) return ORN_ERR_INVALID_ARGUMENT;
-    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED ||
+    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED_MEGA ||
         s->triangle_test > ORN_TRIANGLE_WATERTIGHT || s->pixel_order > ORN_PIXEL_ORDER_RASTER ||
         s->sampler > ORN_SAMPLER_SOBOL)
         return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics, kernel or triangle test");
@@ -1055,7 +967,7 @@ int orn_render(orn_context* ctx) {
     const uint32_t passes = std::max<uint32_t>(ctx->state.iterations, 1u);
     const float ci_start = ctx->current_iteration + 1.0f;
     // a cached frame takes cache_streams() samples per pixel
-    ctx->current_iteration += (float)passes * (ctx->state.kernel == ORN_KERNEL_CACHED ? cache_streams(ctx) : 1u);
+    ctx->current_iteration += (float)passes * (is_cached(ctx) ? cache_streams(ctx) : 1u);
     uint32_t chunk = ctx->state.spp_per_launch;
     if (chunk == 0) chunk = passes <= 64 ? passes : 32;
     RenderLaunch p;
@@ -1071,11 +983,7 @@ int orn_render(orn_context* ctx) {
     p.shade_threshold = orn::kShadeThreshold;
     if (ctx->counters_enabled)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long), ctx->stream));
-    if (ctx->state.kernel == ORN_KERNEL_WAVEFRONT) {
-        st = ensure_wavefront(ctx);
-        if (st) return st;
-    }
-    if (ctx->state.kernel == ORN_KERNEL_CACHED) {
+    if (is_cached(ctx)) {
         if (!ctx->cache)
             return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "ORN_KERNEL_CACHED needs a cache (orn_attach_cache)");
         st = ensure_cache_buffers(ctx);
@@ -1093,17 +1001,17 @@ int orn_render(orn_context* ctx) {
         p.cp = make_params(ctx, ci_start + (float)done);
         p.spp = n;
         p.do_post = (done + n == passes) ? 1u : 0u;
+        use_pixel_order(ctx, &p);
         if (ctx->state.kernel == ORN_KERNEL_WAVEFRONT) {
-            st = render_wavefront_sweep(ctx, p.cp, n, p.do_post != 0);
-            if (st) return st;
+            ORN_CUDA(ctx, orn::launch_wave(p, (int)ctx->state.semantics, ctx->counters_enabled,
+                                           render_fast_slabs(ctx), ctx->stream));
         } else {
-            use_pixel_order(ctx, &p);
             ORN_CUDA(ctx, orn::launch_mega(p, (int)ctx->state.semantics, orn::MATH_PORTABLE,
                                            ctx->counters_enabled, render_fast_slabs(ctx), ctx->stream));
-            ctx->launches++;
-            st = update_pixel_order(ctx, p);
-            if (st) return st;
         }
+        ctx->launches++;
+        st = update_pixel_order(ctx, p);
+        if (st) return st;
         done += n;
     }
     ORN_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));

@@ -22,21 +22,6 @@ namespace orn {
 enum LaneMode { LANE_IDLE = 0, LANE_TRAVERSE = 1, LANE_SHADE = 2, LANE_DONE = 3 };
 
 
-// Solid-angle density of the reference's lambertian scatter direction
-// w = normalize(n + s), s = normalize(in_unit_sphere()) (material.hip.h,
-// random.hip.h), whose polar angle about the world z axis is uniform in
-// [0, pi]: p_s(s) = 1 / (2 pi^2 sin(theta_s)).  The map s -> w takes the unit
-// sphere around n (through the origin) to directions with cos(a) = n.w and
-// |n + s| = 2 cos(a), so p(w) = 4 cos(a) p_s(s) with s = 2 cos(a) w - n.
-// (The direction is not cosine-distributed.)
-__device__ __forceinline__ float scatter_pdf(f3 n, f3 w) {
-    const float ca = dot(n, w);
-    if (!(ca > 0.0f)) return 0.0f;
-    const f3 sv = sub(scale(2.0f * ca, w), n);
-    const float sin_s = fmaxf(sqrtf(sv.x * sv.x + sv.y * sv.y), 1e-7f);
-    return 2.0f * ca / (9.8696044f * sin_s);
-}
-
 // Per-pixel accumulation: FP32 RGBA as the reference keeps it
 // (pathtracer.hip.cpp:148-153), or FP64 for the high-sample-count oracle
 // render (orn_render_f64), where only the accumulation is double.

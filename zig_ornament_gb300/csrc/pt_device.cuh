@@ -675,6 +675,21 @@ __device__ __forceinline__ f3 trace_sample(const SceneDev& sc, const orn_constan
     return color;
 }
 
+// Solid-angle density of the reference's lambertian scatter direction
+// w = normalize(n + s), s = normalize(in_unit_sphere()) (material.hip.h,
+// random.hip.h), whose polar angle about the world z axis is uniform in
+// [0, pi]: p_s(s) = 1 / (2 pi^2 sin(theta_s)).  The map s -> w takes the unit
+// sphere around n (through the origin) to directions with cos(a) = n.w and
+// |n + s| = 2 cos(a), so p(w) = 4 cos(a) p_s(s) with s = 2 cos(a) w - n.
+// (The direction is not cosine-distributed.)
+__device__ __forceinline__ float scatter_pdf(f3 n, f3 w) {
+    const float ca = dot(n, w);
+    if (!(ca > 0.0f)) return 0.0f;
+    const f3 sv = sub(scale(2.0f * ca, w), n);
+    const float sin_s = fmaxf(sqrtf(sv.x * sv.x + sv.y * sv.y), 1e-7f);
+    return 2.0f * ca / (9.8696044f * sin_s);
+}
+
 // post_processing (pathtracer.hip.cpp:58-70; pathtracer.wgsl:81-93)
 template <int SEM, int MATH>
 __device__ __forceinline__ float4 post_process(float4 acc, float ci, float inv_gamma) {

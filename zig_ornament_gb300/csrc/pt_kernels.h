@@ -204,8 +204,10 @@ struct WaveLaunch {
 constexpr int kFetchThreshold = ORN_FETCH_THRESHOLD;
 
 cudaError_t launch_mega(const RenderLaunch& p, int semantics, int math, bool count, bool fast, cudaStream_t s);
-// Cached megakernel launch (one sample per pixel, see CacheLaunch).
+// Cached frame launch (one sample per pixel and stream, see CacheLaunch), on
+// the megakernel or the persistent wavefront (wave_cached.cu).
 cudaError_t launch_mega_cached(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s);
+cudaError_t launch_wave_cached(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s);
 cudaError_t launch_mega_f64(const RenderLaunch& p, int semantics, bool fast, cudaStream_t s);
 // relMSE = mean over pixels and RGB of (x - r)^2 / (r^2 + 1e-2), with x the
 // per-pixel mean of `acc` (FP32 RGBA sums, or FP64 when acc64) and r of
@@ -213,6 +215,9 @@ cudaError_t launch_mega_f64(const RenderLaunch& p, int semantics, bool fast, cud
 // pixels to out[1], both FP64 and zeroed by the caller.
 cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* ref64, uint32_t n,
                           double* out, cudaStream_t s);
+// The persistent wavefront (wave.cu): one launch renders p.spp passes of
+// every pixel, like launch_mega.
+cudaError_t launch_wave(const RenderLaunch& p, int semantics, bool count, bool fast, cudaStream_t s);
 cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, int math, bool count,
                             cudaStream_t s);
 cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, bool fast, cudaStream_t s);

@@ -26,7 +26,8 @@ namespace orn {
 enum { SEM_HIP = 0, SEM_WGSL = 1 };          // enum orn_semantics
 enum { MATH_PORTABLE = 0, MATH_DEVICE = 1 };  // transcendental implementation
 // Error bits written to the context's device error word.
-enum { ERR_STACK = 1u, ERR_VISITS = 2u, ERR_MMA = 4u };   // ERR_MMA: a tensor-core wait timed out
+// ERR_MMA: a tensor-core wait timed out; ERR_WAIT: a wavefront queue wait timed out
+enum { ERR_STACK = 1u, ERR_VISITS = 2u, ERR_MMA = 4u, ERR_WAIT = 8u };
 constexpr uint32_t kRefIndexMask = 0x3FFFFFFFu;
 
 struct TexDesc {

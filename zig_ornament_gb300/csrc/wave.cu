@@ -1,0 +1,283 @@
+// wave.cu — the persistent wavefront: per-block path pools with ray and hit
+// queues in shared memory.
+//
+// The reference's render loop (src/hip_backend/path_tracer.zig:121-133,
+// one launch of path_tracing_kernal per pass, per-pixel work in
+// src/hip_backend/kernels/pathtracer.hip.cpp:72-154) is run as one
+// persistent launch.  Each block owns a pool of P path slots in shared
+// memory and two queues of slot indices:
+//
+//   ray queue  slots whose next ray is ready to trace;
+//   hit queue  slots whose ray was traced (or that need a pixel).
+//
+// Every warp runs the same loop (wave_queue.cuh, wave_warp) and switches
+// between two kinds of work.  While any of its lanes has a ray in flight it
+// traverses: idle lanes take the next rays from the ray queue
+// (ballot-compacted, one reservation per warp), each lane visits BVH nodes
+// (walker_step, the megakernel's traversal) and, when its ray is done,
+// writes the hit record into the slot and appends the slot to the hit
+// queue.  A warp whose lanes have all run out of rays shades: it takes 32
+// slots from the hit queue and runs the path logic with a full warp —
+// material scatter and the next bounce, or the sample's accumulation and
+// the next sample's camera ray, or the pixel's completion (accumulation,
+// RNG state, framebuffer, traversal cost) and the next pixel from the
+// launch's counter (in the longest-first order when one is given).  New
+// rays go to the ray queue.
+//
+// Against the megakernel this separates the two kinds of work: a lane whose
+// ray finished no longer waits for the rest of its warp to finish theirs
+// before it is shaded, and shading code (material scatter, portable
+// transcendentals) runs on full warps instead of the few lanes that happen
+// to be ready.  A pixel's samples still run in order in its slot with the
+// pixel's RNG state, so every pixel is bit-identical to the reference's
+// passes.  Every wait (an entry not yet written, a position not yet
+// cleared, no work while the block is not finished) is bounded by
+// %globaltimer; a wait that runs out sets ERR_WAIT, and every warp of the
+// block returns.
+#include <cuda_fp16.h>
+
+#include "wave_queue.cuh"
+
+namespace orn {
+
+using namespace wave;
+
+namespace {
+
+// The block's path pool (structure of arrays in dynamic shared memory).
+template <int P>
+struct Pool {
+    uint32_t gid[P], k[P], bounce[P], rng[P], steps[P], flag[P];
+    float acc[4][P];
+    float color[3][P];
+    float ro[3][P], rd[3][P];
+    float t[P], u[P], v[P];
+    uint32_t material[P], type[P], inv[P], tri[P];
+    uint32_t rq[P], hq[P];
+    uint32_t rq_head, rq_tail, hq_head, hq_tail;
+    uint32_t active;      // slots not retired
+    uint32_t exhausted;   // the launch's pixel counter ran out
+    uint32_t abort;       // a bounded wait ran out
+};
+
+}  // namespace
+
+#ifndef ORN_WAVE_MIN_BLOCKS
+#define ORN_WAVE_MIN_BLOCKS 3
+#endif
+
+template <int SEM, bool COUNT, bool FAST, int NW, int P>
+__global__ void __launch_bounds__(32 * NW, ORN_WAVE_MIN_BLOCKS)
+wave_kernel(RenderLaunch p) {
+    extern __shared__ __align__(16) unsigned char wave_smem[];
+    Pool<P>& pool = *reinterpret_cast<Pool<P>*>(wave_smem);
+    uint32_t* sstack = reinterpret_cast<uint32_t*>(wave_smem + ((sizeof(Pool<P>) + 15) / 16) * 16);
+    const unsigned kFull = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    pool_init<P>(pool);
+
+    uint32_t err = 0;
+    VisitCount vc = {0, 0, 0, 0, 0};
+    SampleCount scn = {0, 0, 0, 0};
+    const uint32_t W = p.cp.width, H = p.cp.height;
+    const float ci0 = p.cp.current_iteration;
+
+    // The path logic of one shading round: the lane's slot (or kEmpty) was
+    // taken from the hit queue; new rays go to the ray queue.
+    auto shade = [&](uint32_t slot) -> bool {
+        bool emit = false, need = false;
+        uint32_t gid = 0, k = 0, bounce = 0;
+        Rng rng{0};
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        f3 ro = mk(0.0f, 0.0f, 0.0f), rd = ro, color = ro;
+        // Starts samples k.. of the slot's pixel (depth-0 samples finish at
+        // once); true when a camera ray was made, false when the pixel is
+        // complete (its results are then written).
+        auto start_samples = [&]() -> bool {
+            while (k < p.spp) {
+                camera_ray<MATH_PORTABLE>(p.cp, gid % W, gid / W, rng, &ro, &rd);
+                color = mk(1.0f, 1.0f, 1.0f);
+                bounce = 0;
+                if (p.cp.depth > 0) return true;
+                const float ci = ci0 + (float)k;
+                if (ci > 1.0f) acc = make_float4(acc.x + color.x, acc.y + color.y, acc.z + color.z, acc.w + 1.0f);
+                else acc = make_float4(color.x, color.y, color.z, 1.0f);
+                ++k;
+            }
+            p.acc[gid] = acc;
+            p.rng[gid] = rng.state;
+            if (p.cost) p.cost[gid] = pool.steps[slot];
+            if (p.do_post) {
+                const uint32_t x = gid % W, y = gid / W;
+                const uint32_t fbi = p.cp.flip_y != 0 ? W * (H - y - 1) + x : gid;
+                p.fb[fbi] = post_process<SEM, MATH_PORTABLE>(acc, ci0 + (float)(p.spp - 1), p.cp.inverted_gamma);
+            }
+            return false;
+        };
+        if (slot != kEmpty) {
+            if (pool.flag[slot] == NEED_PIXEL) {
+                need = true;
+            } else {
+                gid = pool.gid[slot];
+                k = pool.k[slot];
+                bounce = pool.bounce[slot];
+                rng.state = pool.rng[slot];
+                acc = make_float4(pool.acc[0][slot], pool.acc[1][slot], pool.acc[2][slot], pool.acc[3][slot]);
+                color = mk(pool.color[0][slot], pool.color[1][slot], pool.color[2][slot]);
+                ro = mk(pool.ro[0][slot], pool.ro[1][slot], pool.ro[2][slot]);
+                rd = mk(pool.rd[0][slot], pool.rd[1][slot], pool.rd[2][slot]);
+                const uint32_t flag = pool.flag[slot];
+                bool cont;
+                if (flag != HIT_ANY) {
+                    color = flag == HIT_FAILED ? mk(0.0f, 0.0f, 0.0f) : sky_color(color, rd);
+                    cont = false;
+                } else {
+                    HitRec h;
+                    h.t = pool.t[slot];
+                    h.material = pool.material[slot];
+                    h.type = pool.type[slot];
+                    h.inv = pool.inv[slot];
+                    h.tri = pool.tri[slot];
+                    h.u = pool.u[slot];
+                    h.v = pool.v[slot];
+                    cont = shade_hit<SEM, MATH_PORTABLE, COUNT>(p.scene, p.cp, rng, h, &ro, &rd, &color, &scn);
+                }
+                if (cont && ++bounce < p.cp.depth) {
+                    emit = true;
+                } else {
+                    const float ci = ci0 + (float)k;
+                    if (ci > 1.0f) acc = make_float4(acc.x + color.x, acc.y + color.y, acc.z + color.z, acc.w + 1.0f);
+                    else acc = make_float4(color.x, color.y, color.z, 1.0f);
+                    ++k;
+                    emit = start_samples();
+                    need = !emit;
+                }
+            }
+        }
+        // Lanes whose slot needs a pixel take the next ones (one atomic per
+        // warp); a depth-0 pixel completes at once and asks again.
+        for (;;) {
+            const unsigned nm = __ballot_sync(kFull, need);
+            if (nm == 0u) break;
+            if (warp_flag(vload(pool.exhausted) != 0u)) {
+                if (need) {
+                    atomicSub(&pool.active, 1u);
+                    need = false;
+                    slot = kEmpty;
+                }
+                continue;
+            }
+            const unsigned leader = __ffs(nm) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(p.work_counter, (unsigned)__popc(nm));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + __popc(nm) >= p.pixel_count && lane == leader) atomicExch(&pool.exhausted, 1u);
+            if (need) {
+                const uint32_t mine = base + __popc(nm & ((1u << lane) - 1u));
+                if (mine < p.pixel_count) {
+                    gid = p.order ? p.order[mine] : mine;
+                    rng.state = p.rng[gid];
+                    acc = ci0 > 1.0f ? p.acc[gid] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    k = 0;
+                    pool.steps[slot] = 0;
+                    emit = start_samples();
+                    need = !emit;
+                } else {
+                    atomicSub(&pool.active, 1u);
+                    need = false;
+                    slot = kEmpty;
+                }
+            }
+        }
+        if (emit) {
+            if (COUNT) scn.rays++;
+            pool.gid[slot] = gid;
+            pool.k[slot] = k;
+            pool.bounce[slot] = bounce;
+            pool.rng[slot] = rng.state;
+            pool.acc[0][slot] = acc.x;
+            pool.acc[1][slot] = acc.y;
+            pool.acc[2][slot] = acc.z;
+            pool.acc[3][slot] = acc.w;
+            pool.color[0][slot] = color.x;
+            pool.color[1][slot] = color.y;
+            pool.color[2][slot] = color.z;
+            pool.ro[0][slot] = ro.x;
+            pool.ro[1][slot] = ro.y;
+            pool.ro[2][slot] = ro.z;
+            pool.rd[0][slot] = rd.x;
+            pool.rd[1][slot] = rd.y;
+            pool.rd[2][slot] = rd.z;
+            __threadfence_block();
+        }
+        return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
+    };
+    wave_warp<COUNT, FAST, false, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err, shade);
+
+    if (err) atomicOr(p.error, err);
+    if (COUNT) {
+        atomicAdd(p.counters + 1, (unsigned long long)scn.rays);
+        atomicAdd(p.counters + 2, (unsigned long long)vc.visits);
+        atomicAdd(p.counters + 3, (unsigned long long)vc.internal);
+        atomicAdd(p.counters + 4, (unsigned long long)vc.sphere);
+        atomicAdd(p.counters + 5, (unsigned long long)vc.mesh);
+        atomicAdd(p.counters + 6, (unsigned long long)vc.tri);
+        atomicAdd(p.counters + 7, (unsigned long long)scn.sphere_hits);
+        atomicAdd(p.counters + 8, (unsigned long long)scn.mesh_hits);
+        atomicAdd(p.counters + 9, (unsigned long long)scn.textured);
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            atomicAdd(p.counters + 0, (unsigned long long)p.spp * p.pixel_count);
+    }
+}
+
+// ---- host-side launcher ------------------------------------------------------------
+namespace {
+
+// warps per block and path slots per block (the slots outnumber the lanes,
+// so lanes find rays while other paths wait to be shaded)
+#ifndef ORN_WAVE_WARPS
+#define ORN_WAVE_WARPS 8
+#endif
+#ifndef ORN_WAVE_SLOTS
+#define ORN_WAVE_SLOTS 320
+#endif
+constexpr int kWaveW = ORN_WAVE_WARPS, kWaveP = ORN_WAVE_SLOTS;
+
+template <int SEM, bool COUNT, bool FAST>
+cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
+    constexpr int kBlock = 32 * kWaveW;
+    constexpr size_t kSmem = ((sizeof(Pool<kWaveP>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * kBlock;
+    static int blocks_per_sm = 0, sms = 0;
+    auto kern = wave_kernel<SEM, COUNT, FAST, kWaveW, kWaveP>;
+    // more than 48 KB of dynamic shared memory: an opt-in per device
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+    if (e != cudaSuccess) return e;
+    if (blocks_per_sm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kBlock, kSmem);
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    // enough blocks for every pixel to have a slot, at most one wave of resident blocks
+    uint32_t need = (p.pixel_count + kWaveP - 1) / kWaveP;
+    uint32_t grid = (uint32_t)(blocks_per_sm * sms);
+    if (need < grid) grid = need;
+    e = cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kBlock, kSmem, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_wave(const RenderLaunch& p, int semantics, bool count, bool fast, cudaStream_t s) {
+    if (semantics == SEM_WGSL) {
+        if (fast) return count ? launch_wave_t<SEM_WGSL, true, true>(p, s) : launch_wave_t<SEM_WGSL, false, true>(p, s);
+        return count ? launch_wave_t<SEM_WGSL, true, false>(p, s) : launch_wave_t<SEM_WGSL, false, false>(p, s);
+    }
+    if (fast) return count ? launch_wave_t<SEM_HIP, true, true>(p, s) : launch_wave_t<SEM_HIP, false, true>(p, s);
+    return count ? launch_wave_t<SEM_HIP, true, false>(p, s) : launch_wave_t<SEM_HIP, false, false>(p, s);
+}
+
+}  // namespace orn
