@@ -118,6 +118,9 @@ def parse():
                         "streams, Sobol sampler, SAH tree, train_shift 3, lr 5e-3, 64 steps per frame)")
     p.add_argument("--scene", default="instanced", choices=["instanced", "closed-room"],
                    help="cached-frames: the scene")
+    p.add_argument("--cached-kernel", default="wavefront", choices=["wavefront", "mega"],
+                   help="the cached renderer's kernel (relmse and cached-frames): the persistent wavefront "
+                        "(KERNEL_CACHED) or the megakernel (KERNEL_CACHED_MEGA)")
     return p.parse_args()
 
 
@@ -671,7 +674,8 @@ def crossing_time(curve, target):
 
 
 def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=None, warmup=64, methods=None,
-                   ref=None, streams=8, batched_warmup_spp=16, batched_sobol=True, batched_cfg=None):
+                   ref=None, streams=8, batched_warmup_spp=16, batched_sobol=True, batched_cfg=None,
+                   cached_kernel=None):
     """GPU time each renderer needs to bring the relMSE against an FP64
     `ref_spp`-sample oracle (orn_render_f64 with the plain megakernel on the
     parity tree) down to `target`:
@@ -714,10 +718,12 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         rr.close()
     ref_s = time.time() - t0
     out = {"resolution": f"{w}x{h}", "depth": depth, "reference_spp": ref_spp, "reference_seconds": round(ref_s, 1),
-           "reference": "plain megakernel, parity tree, FP64 accumulation"}
+           "reference": "plain megakernel, parity tree, FP64 accumulation",
+           "cached_kernel": "megakernel" if cached_kernel == _lib.KERNEL_CACHED_MEGA else "persistent wavefront"}
     on_sah = ("plain_sah", "cached_tuned", "cached_batched")
     for method in (methods or ("plain", "plain_sah", "light_sampling", "cached", "cached_tuned", "cached_batched")):
-        kernel = _lib.KERNEL_MEGA if method in ("plain", "plain_sah") else _lib.KERNEL_CACHED
+        ck = _lib.KERNEL_CACHED if cached_kernel is None else cached_kernel
+        kernel = _lib.KERNEL_MEGA if method in ("plain", "plain_sah") else ck
         tuned = method in ("cached_tuned", "cached_batched")
         if method in on_sah and bvh_sah is None:
             bvh_sah = ornament.Bvh(scene, row_major_transforms=True, builder="sah")
@@ -727,7 +733,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             st.sampler = _lib.SAMPLER_SOBOL if batched_sobol else _lib.SAMPLER_PCG
         cache = None
         t = 0.0
-        if kernel == _lib.KERNEL_CACHED:
+        if kernel != _lib.KERNEL_MEGA:
             if method == "light_sampling":
                 cfg = {"train_shift": 0, "steps_per_frame": 0}
             elif method == "cached_batched":
@@ -802,8 +808,10 @@ def relmse_block(args):
         todo = (("instanced", args.relmse_width, args.relmse_height, 8), ("closed-room", 640, 360, 8))
     for name, w, h, depth in todo:
         t0 = time.time()
+        from zig_ornament_gb300 import _lib
+        ck = _lib.KERNEL_CACHED_MEGA if args.cached_kernel == "mega" else _lib.KERNEL_CACHED
         res["scenes"][name] = time_to_relmse(name, w, h, args.relmse_target, args.relmse_ref_spp, args.relmse_budget,
-                                             depth=depth)
+                                             depth=depth, cached_kernel=ck)
         res["scenes"][name].pop("_ref")
         res["scenes"][name]["wall_s"] = round(time.time() - t0, 1)
     return res
@@ -820,7 +828,7 @@ def run_cached_frames(args):
     r.set_resolution(args.width, args.height)
     st = ornament.State()
     st.depth = args.depth
-    st.kernel = _lib.KERNEL_CACHED
+    st.kernel = _lib.KERNEL_CACHED_MEGA if args.cached_kernel == "mega" else _lib.KERNEL_CACHED
     cfg = {}
     if args.batched:
         st.spp_per_launch = 8

@@ -10,13 +10,13 @@
 //   ray queue  slots whose next ray is ready to trace;
 //   hit queue  slots whose ray was traced (or that need a pixel).
 //
-// Every warp runs the same loop (wave_queue.cuh, wave_warp) and switches
-// between two kinds of work.  While any of its lanes has a ray in flight it
+// One warp of a block only shades; the others run the same loop
+// (wave_queue.cuh, wave_warp) and switch between two kinds of work.  While any of its lanes has a ray in flight it
 // traverses: idle lanes take the next rays from the ray queue
 // (ballot-compacted, one reservation per warp), each lane visits BVH nodes
 // (walker_step, the megakernel's traversal) and, when its ray is done,
 // writes the hit record into the slot and appends the slot to the hit
-// queue.  A warp whose lanes have all run out of rays shades: it takes 32
+// queue.  A warp whose lanes have all run out of rays shades too: it takes 32
 // slots from the hit queue and runs the path logic with a full warp —
 // material scatter and the next bounce, or the sample's accumulation and
 // the next sample's camera ray, or the pixel's completion (accumulation,
@@ -66,7 +66,7 @@ struct Pool {
 #define ORN_WAVE_MIN_BLOCKS 3
 #endif
 
-template <int SEM, bool COUNT, bool FAST, int NW, int P>
+template <int SEM, bool COUNT, bool FAST, int NW, int NS, int P>
 __global__ void __launch_bounds__(32 * NW, ORN_WAVE_MIN_BLOCKS)
 wave_kernel(RenderLaunch p) {
     extern __shared__ __align__(16) unsigned char wave_smem[];
@@ -212,7 +212,8 @@ wave_kernel(RenderLaunch p) {
         }
         return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
     };
-    wave_warp<COUNT, FAST, false, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err, shade);
+    wave_warp<COUNT, FAST, false, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
+                                     (threadIdx.x >> 5) < (uint32_t)NS, shade);
 
     if (err) atomicOr(p.error, err);
     if (COUNT) {
@@ -241,14 +242,18 @@ namespace {
 #ifndef ORN_WAVE_SLOTS
 #define ORN_WAVE_SLOTS 320
 #endif
-constexpr int kWaveW = ORN_WAVE_WARPS, kWaveP = ORN_WAVE_SLOTS;
+// warps of a block that only shade
+#ifndef ORN_WAVE_SHADERS
+#define ORN_WAVE_SHADERS 1
+#endif
+constexpr int kWaveW = ORN_WAVE_WARPS, kWaveP = ORN_WAVE_SLOTS, kWaveS = ORN_WAVE_SHADERS;
 
 template <int SEM, bool COUNT, bool FAST>
 cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
     constexpr int kBlock = 32 * kWaveW;
     constexpr size_t kSmem = ((sizeof(Pool<kWaveP>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * kBlock;
     static int blocks_per_sm = 0, sms = 0;
-    auto kern = wave_kernel<SEM, COUNT, FAST, kWaveW, kWaveP>;
+    auto kern = wave_kernel<SEM, COUNT, FAST, kWaveW, kWaveS, kWaveP>;
     // more than 48 KB of dynamic shared memory: an opt-in per device
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
     if (e != cudaSuccess) return e;

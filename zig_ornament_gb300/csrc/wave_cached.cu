@@ -7,7 +7,8 @@
 // and records the network inputs at the cache vertex and the radiance that
 // left it.  The path logic is the cached megakernel's (megakernel.cu,
 // CACHE = true), operation for operation; what changes is where it runs.
-// The block's warps run wave_warp (wave_queue.cuh) and switch between
+// Two warps of a block only shade; the others run wave_warp (wave_queue.cuh)
+// and switch between
 //
 //   traversal   every ray of the block's paths — scattered rays and the
 //               any-hit shadow rays of light samples (ANY);
@@ -64,7 +65,7 @@ __device__ __forceinline__ void st3(float (&a)[3][P], uint32_t i, f3 v) {
 
 }  // namespace
 
-template <int SEM, bool FAST, bool SOBOL, int NW, int P>
+template <int SEM, bool FAST, bool SOBOL, int NW, int NS, int P>
 __global__ void __launch_bounds__(32 * NW, 2)
 wave_cached_kernel(RenderLaunch p) {
     extern __shared__ __align__(16) unsigned char wave_smem[];
@@ -473,7 +474,8 @@ wave_cached_kernel(RenderLaunch p) {
         }
         return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
     };
-    wave_warp<false, FAST, true, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err, shade);
+    wave_warp<false, FAST, true, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
+                                    (threadIdx.x >> 5) < (uint32_t)NS, shade);
     if (err) atomicOr(p.error, err);
 }
 
@@ -486,14 +488,17 @@ namespace {
 #ifndef ORN_WAVE_CACHED_SLOTS
 #define ORN_WAVE_CACHED_SLOTS 320
 #endif
-constexpr int kCachedW = ORN_WAVE_CACHED_WARPS, kCachedP = ORN_WAVE_CACHED_SLOTS;
+#ifndef ORN_WAVE_CACHED_SHADERS
+#define ORN_WAVE_CACHED_SHADERS 2
+#endif
+constexpr int kCachedW = ORN_WAVE_CACHED_WARPS, kCachedP = ORN_WAVE_CACHED_SLOTS, kCachedS = ORN_WAVE_CACHED_SHADERS;
 
 template <int SEM, bool FAST, bool SOBOL>
 cudaError_t launch_t(const RenderLaunch& p, cudaStream_t s) {
     constexpr int kBlock = 32 * kCachedW;
     constexpr size_t kSmem = ((sizeof(CPool<kCachedP>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * kBlock;
     static int blocks_per_sm = 0, sms = 0;
-    auto kern = wave_cached_kernel<SEM, FAST, SOBOL, kCachedW, kCachedP>;
+    auto kern = wave_cached_kernel<SEM, FAST, SOBOL, kCachedW, kCachedS, kCachedP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
     if (e != cudaSuccess) return e;
     if (blocks_per_sm == 0) {

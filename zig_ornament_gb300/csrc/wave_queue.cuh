@@ -134,13 +134,16 @@ __device__ __forceinline__ uint32_t q_pop(uint32_t* q, uint32_t* head, const uin
 //     takes new rays.
 // So traversal keeps every lane it can busy, and shading runs on full warps
 // by whichever warps have run out of rays, in whatever proportion the scene
-// needs.  With ANY (shadow rays of the cached renderer) the slot also gives
+// needs.  A `shade_only` warp never traverses: it shades whatever hits are
+// queued (the kernels keep one or two such warps per block, so that the ray
+// queue is refilled while every other warp still has rays in flight).  With ANY (shadow rays of the cached renderer) the slot also gives
 // the ray's t_max and occluder test (pool.ray_tmax, occl_inv, occl_t).
 // Returns when the block is finished (no pixel left, every slot retired)
 // or a wait ran out (pool.abort, ERR_WAIT).
 template <bool COUNT, bool FAST, bool ANY, int P, class Pool, class Shade>
 __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uint32_t* sstack, int stride,
-                                          uint32_t lane, VisitCount& vc, uint32_t& err, Shade&& shade) {
+                                          uint32_t lane, VisitCount& vc, uint32_t& err, bool shade_only,
+                                          Shade&& shade) {
     const unsigned kFull = 0xffffffffu;
     TravStack<kSmemStack> stack;
     stack.sstack = sstack;
@@ -161,7 +164,7 @@ __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uin
         if (__ballot_sync(kFull, slot != kEmpty) == 0u) {
             // no ray in flight: shade, or take rays, or wait
             const uint32_t nh = q_count(&pool.hq_head, &pool.hq_tail);
-            const uint32_t nr = q_count(&pool.rq_head, &pool.rq_tail);
+            const uint32_t nr = shade_only ? 0u : q_count(&pool.rq_head, &pool.rq_tail);
             if (nh >= 32u || (nh > 0u && nr == 0u)) {
                 const uint32_t s = q_pop<P>(pool.hq, &pool.hq_head, &pool.hq_tail, kFull, lane, &ok);
                 if (!__all_sync(kFull, ok)) { fail(); break; }
