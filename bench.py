@@ -118,9 +118,9 @@ def parse():
                         "streams, Sobol sampler, SAH tree, train_shift 3, lr 5e-3, 64 steps per frame)")
     p.add_argument("--scene", default="instanced", choices=["instanced", "closed-room"],
                    help="cached-frames: the scene")
-    p.add_argument("--cached-kernel", default="wavefront", choices=["wavefront", "mega"],
-                   help="the cached renderer's kernel (relmse and cached-frames): the persistent wavefront "
-                        "(KERNEL_CACHED) or the megakernel (KERNEL_CACHED_MEGA)")
+    p.add_argument("--cached-kernel", default="mega", choices=["mega", "wavefront"],
+                   help="the cached renderer's kernel (relmse and cached-frames): the megakernel "
+                        "(KERNEL_CACHED, the faster) or the persistent wavefront (KERNEL_CACHED_WAVEFRONT)")
     return p.parse_args()
 
 
@@ -690,7 +690,10 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
       cached_batched  `streams` sample streams per pixel batched into each
                       frame's launch (orn_state.spp_per_launch), the Sobol
                       sampler, training slots for 1/8 of the samples at lr
-                      5e-3, a 16-sample warm-up, SAH tree.
+                      5e-3, a 16-sample warm-up, SAH tree;
+      cached_batched_wavefront  the same on the persistent wavefront
+                      (KERNEL_CACHED_WAVEFRONT; the others use `cached_kernel`,
+                      the megakernel by default).
     Progressive rendering in growing chunks; relMSE (orn_relmse, FP64 on the
     GPU) is read between chunks outside the timed renders; the crossing is
     interpolated log-linearly between the two chunks around it, or
@@ -719,16 +722,20 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
     ref_s = time.time() - t0
     out = {"resolution": f"{w}x{h}", "depth": depth, "reference_spp": ref_spp, "reference_seconds": round(ref_s, 1),
            "reference": "plain megakernel, parity tree, FP64 accumulation",
-           "cached_kernel": "megakernel" if cached_kernel == _lib.KERNEL_CACHED_MEGA else "persistent wavefront"}
-    on_sah = ("plain_sah", "cached_tuned", "cached_batched")
-    for method in (methods or ("plain", "plain_sah", "light_sampling", "cached", "cached_tuned", "cached_batched")):
+           "cached_kernel": "persistent wavefront" if cached_kernel == _lib.KERNEL_CACHED_WAVEFRONT else "megakernel"}
+    on_sah = ("plain_sah", "cached_tuned", "cached_batched", "cached_batched_wavefront")
+    for method in (methods or ("plain", "plain_sah", "light_sampling", "cached", "cached_tuned", "cached_batched",
+                               "cached_batched_wavefront")):
         ck = _lib.KERNEL_CACHED if cached_kernel is None else cached_kernel
+        if method == "cached_batched_wavefront":
+            ck = _lib.KERNEL_CACHED_WAVEFRONT
         kernel = _lib.KERNEL_MEGA if method in ("plain", "plain_sah") else ck
-        tuned = method in ("cached_tuned", "cached_batched")
+        batched = method.startswith("cached_batched")
+        tuned = method in ("cached_tuned", "cached_batched", "cached_batched_wavefront")
         if method in on_sah and bvh_sah is None:
             bvh_sah = ornament.Bvh(scene, row_major_transforms=True, builder="sah")
         r, st = renderer(kernel, bvh_sah if method in on_sah else None)
-        if method == "cached_batched":
+        if batched:
             st.spp_per_launch = streams
             st.sampler = _lib.SAMPLER_SOBOL if batched_sobol else _lib.SAMPLER_PCG
         cache = None
@@ -736,7 +743,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         if kernel != _lib.KERNEL_MEGA:
             if method == "light_sampling":
                 cfg = {"train_shift": 0, "steps_per_frame": 0}
-            elif method == "cached_batched":
+            elif batched:
                 # training slots for 1/8 of the samples, filled at cache
                 # vertices; one pass over the frame's training data (steps
                 # capped by the slots)
@@ -749,7 +756,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             r.attach_cache(cache)
         if method.startswith("cached"):
             # warm-up training, then the accumulation restarts
-            if method == "cached_batched":
+            if batched:
                 st.iterations = max(1, -(-batched_warmup_spp // streams))
             else:
                 st.iterations = 32 if tuned else warmup
@@ -763,7 +770,7 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
             r.set_state(st.to_struct())
             r.render()
             t += r.last_render_ms() / 1e3
-            n += chunk * (streams if method == "cached_batched" else 1)
+            n += chunk * (streams if batched else 1)
             e = r.relmse(ref)
             curve.append((t, n, e))
             if e <= target or t >= budget_s:
@@ -777,12 +784,13 @@ def time_to_relmse(name, w, h, target, ref_spp, budget_s, depth=8, cache_cfg=Non
         r.close()
         if cache is not None:
             cache.close()
-    if "cached_batched" in out:
-        out["cached_batched"]["streams"] = streams
-    for m in ("plain_sah", "cached", "cached_tuned", "cached_batched", "light_sampling"):
+    for m in ("cached_batched", "cached_batched_wavefront"):
+        if m in out:
+            out[m]["streams"] = streams
+    for m in ("plain_sah", "cached", "cached_tuned", "cached_batched", "cached_batched_wavefront", "light_sampling"):
         if m in out and "plain" in out:
             out[f"speedup_{m}_vs_plain"] = round(out["plain"]["seconds"] / out[m]["seconds"], 3)
-    for m in ("cached_tuned", "cached_batched"):
+    for m in ("cached_tuned", "cached_batched", "cached_batched_wavefront"):
         if m in out and "plain_sah" in out:
             out[f"speedup_{m}_vs_plain_same_tree"] = round(out["plain_sah"]["seconds"] / out[m]["seconds"], 3)
     if "speedup_cached_batched_vs_plain_same_tree" in out:
@@ -809,7 +817,7 @@ def relmse_block(args):
     for name, w, h, depth in todo:
         t0 = time.time()
         from zig_ornament_gb300 import _lib
-        ck = _lib.KERNEL_CACHED_MEGA if args.cached_kernel == "mega" else _lib.KERNEL_CACHED
+        ck = _lib.KERNEL_CACHED_WAVEFRONT if args.cached_kernel == "wavefront" else _lib.KERNEL_CACHED
         res["scenes"][name] = time_to_relmse(name, w, h, args.relmse_target, args.relmse_ref_spp, args.relmse_budget,
                                              depth=depth, cached_kernel=ck)
         res["scenes"][name].pop("_ref")
@@ -828,7 +836,7 @@ def run_cached_frames(args):
     r.set_resolution(args.width, args.height)
     st = ornament.State()
     st.depth = args.depth
-    st.kernel = _lib.KERNEL_CACHED_MEGA if args.cached_kernel == "mega" else _lib.KERNEL_CACHED
+    st.kernel = _lib.KERNEL_CACHED_WAVEFRONT if args.cached_kernel == "wavefront" else _lib.KERNEL_CACHED
     cfg = {}
     if args.batched:
         st.spp_per_launch = 8

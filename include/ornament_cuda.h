@@ -167,10 +167,11 @@ enum orn_kernel {
                                    hit queues in shared memory, warps that traverse
                                    or shade (same bits as MEGA) */
     ORN_KERNEL_CACHED = 2,      /* learned radiance cache (orn_attach_cache) on the
-                                   persistent wavefront; biased, not bit-exact with
-                                   the reference */
-    ORN_KERNEL_CACHED_MEGA = 3  /* the same cached renderer on the megakernel (the
-                                   same estimator, path for path) */
+                                   megakernel; biased, not bit-exact with the
+                                   reference */
+    ORN_KERNEL_CACHED_WAVEFRONT = 3  /* the same cached renderer on the persistent
+                                        wavefront (the same estimator, path for
+                                        path) */
 };
 
 /* State, src/state.zig:3-23 (resolution set by orn_set_resolution). */

@@ -305,8 +305,8 @@ def test_sobol_sampler_is_unbiased():
 @pytest.mark.parametrize("sampler", [_lib.SAMPLER_PCG, _lib.SAMPLER_SOBOL], ids=["pcg", "sobol"])
 @pytest.mark.parametrize("semantics", [_lib.SEMANTICS_HIP, _lib.SEMANTICS_WGSL], ids=["hip", "wgsl"])
 def test_cached_wavefront_matches_cached_megakernel(sampler, semantics):
-    """The cached renderer on the persistent wavefront (KERNEL_CACHED) runs
-    the cached megakernel's path logic (KERNEL_CACHED_MEGA) operation for
+    """The cached renderer on the persistent wavefront (KERNEL_CACHED_WAVEFRONT)
+    runs the cached megakernel's path logic (KERNEL_CACHED) operation for
     operation: with the network's part off (every path a training path,
     train_shift 0, no training steps) and one sample stream, both give the
     same accumulation and RNG states bit for bit over several frames —
@@ -314,7 +314,7 @@ def test_cached_wavefront_matches_cached_megakernel(sampler, semantics):
     w, h = 160, 96
     scene = _cache_scene(w, h)
     out = {}
-    for kernel in (_lib.KERNEL_CACHED_MEGA, _lib.KERNEL_CACHED):
+    for kernel in (_lib.KERNEL_CACHED, _lib.KERNEL_CACHED_WAVEFRONT):
         r, st = _renderer(scene, w, h, kernel)
         st.sampler = sampler
         st.semantics = semantics
@@ -327,7 +327,7 @@ def test_cached_wavefront_matches_cached_megakernel(sampler, semantics):
         r.attach_cache(None)
         r.close()
         cache.close()
-    a, b = out[_lib.KERNEL_CACHED_MEGA], out[_lib.KERNEL_CACHED]
+    a, b = out[_lib.KERNEL_CACHED], out[_lib.KERNEL_CACHED_WAVEFRONT]
     assert a[2] == b[2] == 6.0
     assert np.array_equal(a[1], b[1])
     assert np.array_equal(a[0], b[0])

@@ -368,8 +368,9 @@ def test_sah_tree_renders_like_the_oracle(oracle, kernel):
     r.close()
 
 
-@pytest.mark.parametrize("kernel", [_lib.KERNEL_MEGA, _lib.KERNEL_WAVEFRONT, _lib.KERNEL_CACHED],
-                         ids=["mega", "wavefront", "cached"])
+@pytest.mark.parametrize("kernel", [_lib.KERNEL_MEGA, _lib.KERNEL_WAVEFRONT, _lib.KERNEL_CACHED,
+                                    _lib.KERNEL_CACHED_WAVEFRONT],
+                         ids=["mega", "wavefront", "cached", "cached-wavefront"])
 def test_pixel_order_does_not_change_results(kernel):
     """Longest-first hand-out (orn_state.pixel_order = COST, the default)
     against raster order over several launches: the same bits."""
@@ -380,7 +381,7 @@ def test_pixel_order_does_not_change_results(kernel):
     for order in (_lib.PIXEL_ORDER_RASTER, _lib.PIXEL_ORDER_COST):
         r = ornament.Renderer(bvh, device=0)
         cache = None
-        if kernel == _lib.KERNEL_CACHED:
+        if kernel in (_lib.KERNEL_CACHED, _lib.KERNEL_CACHED_WAVEFRONT):
             # no training steps: float atomics in the weight-gradient sums
             # make trained weights differ in the last bits between runs
             cache = ornament.RadianceCache(seed=1, train_shift=3, steps_per_frame=0)

@@ -33,7 +33,7 @@ CACHE_INPUTS = 10
 CACHE_OUTPUTS = 3
 CACHE_PARAM_COUNT = 33792
 KERNEL_CACHED = 2
-KERNEL_CACHED_MEGA = 3
+KERNEL_CACHED_WAVEFRONT = 3
 BATCH_MAX = 64
 BVH_REFERENCE, BVH_SAH, BVH_LBVH = 0, 1, 2
 TRIANGLE_MOLLER_TRUMBORE, TRIANGLE_WATERTIGHT = 0, 1

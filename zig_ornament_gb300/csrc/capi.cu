@@ -474,7 +474,7 @@ bool render_fast_slabs(const orn_context* ctx) {
 
 // The cached renderer (on the wavefront or the megakernel).
 bool is_cached(const orn_context* ctx) {
-    return ctx->state.kernel == ORN_KERNEL_CACHED || ctx->state.kernel == ORN_KERNEL_CACHED_MEGA;
+    return ctx->state.kernel == ORN_KERNEL_CACHED || ctx->state.kernel == ORN_KERNEL_CACHED_WAVEFRONT;
 }
 
 // Query queue and training slots of the cached renderer, sized for the
@@ -569,10 +569,10 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->cq_count, 0, 4, ctx->stream));
         // slots no training path writes this frame read as "no target" (NaN)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->ct_target, 0xFF, (size_t)ctx->cq_slots * 12, ctx->stream));
-        if (ctx->state.kernel == ORN_KERNEL_CACHED_MEGA)
-            ORN_CUDA(ctx, orn::launch_mega_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
-        else
+        if (ctx->state.kernel == ORN_KERNEL_CACHED_WAVEFRONT)
             ORN_CUDA(ctx, orn::launch_wave_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
+        else
+            ORN_CUDA(ctx, orn::launch_mega_cached(p, (int)ctx->state.semantics, fast, ctx->stream));
         ctx->launches++;
         int st = orn::cache_apply_queries(c, ctx->cq_count, n * streams, ctx->cq_in, ctx->cq_pixel, ctx->cq_thr, ctx->acc,
                                           ctx->d_error, ctx->stream);
@@ -889,7 +889,7 @@ int orn_destroy(orn_context* ctx) {
 
 int orn_set_state(orn_context* ctx, const orn_state* s) {
     if (!ctx || !s) return ORN_ERR_INVALID_ARGUMENT;
-    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED_MEGA ||
+    if (s->semantics > ORN_SEMANTICS_WGSL || s->kernel > ORN_KERNEL_CACHED_WAVEFRONT ||
         s->triangle_test > ORN_TRIANGLE_WATERTIGHT || s->pixel_order > ORN_PIXEL_ORDER_RASTER ||
         s->sampler > ORN_SAMPLER_SOBOL)
         return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "unknown semantics, kernel or triangle test");

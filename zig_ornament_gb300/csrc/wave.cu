@@ -10,14 +10,13 @@
 //   ray queue  slots whose next ray is ready to trace;
 //   hit queue  slots whose ray was traced (or that need a pixel).
 //
-// One warp of a block only shades; the others run the same loop
-// (wave_queue.cuh, wave_warp) and switch between two kinds of work.  While any of its lanes has a ray in flight it
-// traverses: idle lanes take the next rays from the ray queue
-// (ballot-compacted, one reservation per warp), each lane visits BVH nodes
-// (walker_step, the megakernel's traversal) and, when its ray is done,
-// writes the hit record into the slot and appends the slot to the hit
-// queue.  A warp whose lanes have all run out of rays shades too: it takes 32
-// slots from the hit queue and runs the path logic with a full warp —
+// The block's warps (wave_queue.cuh, wave_warp) split the work: seven of the
+// eight traverse — idle lanes take the next rays from the ray queue
+// (ballot-compacted, one reservation per warp) once four of them are idle,
+// each lane visits BVH nodes (walker_step, the megakernel's traversal) and,
+// when its ray is done, writes the hit record into the slot and appends the
+// slot to the hit queue — and one shades: it takes up to 32 slots from the
+// hit queue and runs the path logic with a full warp —
 // material scatter and the next bounce, or the sample's accumulation and
 // the next sample's camera ray, or the pixel's completion (accumulation,
 // RNG state, framebuffer, traversal cost) and the next pixel from the
@@ -213,7 +212,7 @@ wave_kernel(RenderLaunch p) {
         return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
     };
     wave_warp<COUNT, FAST, false, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
-                                     (threadIdx.x >> 5) < (uint32_t)NS, shade);
+                                     (threadIdx.x >> 5) < (uint32_t)NS ? ROLE_SHADE : ROLE_TRAVERSE, shade);
 
     if (err) atomicOr(p.error, err);
     if (COUNT) {
@@ -242,7 +241,7 @@ namespace {
 #ifndef ORN_WAVE_SLOTS
 #define ORN_WAVE_SLOTS 320
 #endif
-// warps of a block that only shade
+// warps of a block that shade (the others traverse)
 #ifndef ORN_WAVE_SHADERS
 #define ORN_WAVE_SHADERS 1
 #endif

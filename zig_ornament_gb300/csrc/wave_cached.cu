@@ -475,7 +475,7 @@ wave_cached_kernel(RenderLaunch p) {
         return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
     };
     wave_warp<false, FAST, true, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
-                                    (threadIdx.x >> 5) < (uint32_t)NS, shade);
+                                    (threadIdx.x >> 5) < (uint32_t)NS ? ROLE_SHADE : ROLE_BOTH, shade);
     if (err) atomicOr(p.error, err);
 }
 

@@ -31,6 +31,9 @@ constexpr int kWaveFetch = ORN_WAVE_FETCH;
 constexpr int kWaveSteps = ORN_WAVE_STEPS;
 constexpr uint64_t kWaitLimitNs = 5000000000ull;   // 5 s: any real wait is microseconds
 enum SlotFlag { HIT_MISS = 0, HIT_ANY = 1, HIT_FAILED = 2, NEED_PIXEL = 3 };
+// What a warp of a wavefront block does (wave_warp): both kinds of work, only
+// shading, or only traversal.
+enum WarpRole { ROLE_BOTH = 0, ROLE_SHADE = 1, ROLE_TRAVERSE = 2 };
 
 __device__ __forceinline__ uint64_t wave_timer() {
     uint64_t t;
@@ -134,16 +137,21 @@ __device__ __forceinline__ uint32_t q_pop(uint32_t* q, uint32_t* head, const uin
 //     takes new rays.
 // So traversal keeps every lane it can busy, and shading runs on full warps
 // by whichever warps have run out of rays, in whatever proportion the scene
-// needs.  A `shade_only` warp never traverses: it shades whatever hits are
-// queued (the kernels keep one or two such warps per block, so that the ray
-// queue is refilled while every other warp still has rays in flight).  With ANY (shadow rays of the cached renderer) the slot also gives
+// needs.  A ROLE_SHADE warp never traverses: it shades whatever hits are
+// queued, so the ray queue is refilled while every other warp still has rays
+// in flight; a ROLE_TRAVERSE warp never shades.  Measured on the 1080p plain
+// workload (7 + 1 warps per block): traversal-only warps beside one shading
+// warp 331 Msamples/s, warps that also shade when they run dry 275; on cached
+// frames, where shading is heavier, two shading warps beside six that do both
+// were fastest.  With ANY (shadow rays of the cached renderer) the slot also gives
 // the ray's t_max and occluder test (pool.ray_tmax, occl_inv, occl_t).
 // Returns when the block is finished (no pixel left, every slot retired)
 // or a wait ran out (pool.abort, ERR_WAIT).
 template <bool COUNT, bool FAST, bool ANY, int P, class Pool, class Shade>
 __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uint32_t* sstack, int stride,
-                                          uint32_t lane, VisitCount& vc, uint32_t& err, bool shade_only,
+                                          uint32_t lane, VisitCount& vc, uint32_t& err, WarpRole role,
                                           Shade&& shade) {
+    const bool shade_only = role == ROLE_SHADE, traverse_only = role == ROLE_TRAVERSE;
     const unsigned kFull = 0xffffffffu;
     TravStack<kSmemStack> stack;
     stack.sstack = sstack;
@@ -165,7 +173,7 @@ __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uin
             // no ray in flight: shade, or take rays, or wait
             const uint32_t nh = q_count(&pool.hq_head, &pool.hq_tail);
             const uint32_t nr = shade_only ? 0u : q_count(&pool.rq_head, &pool.rq_tail);
-            if (nh >= 32u || (nh > 0u && nr == 0u)) {
+            if (!traverse_only && (nh >= 32u || (nh > 0u && nr == 0u))) {
                 const uint32_t s = q_pop<P>(pool.hq, &pool.hq_head, &pool.hq_tail, kFull, lane, &ok);
                 if (!__all_sync(kFull, ok)) { fail(); break; }
                 if (!shade(s)) { fail(); break; }
@@ -173,7 +181,8 @@ __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uin
                 continue;
             }
             if (nr == 0u) {
-                if (nh == 0u && warp_flag(vload(pool.exhausted) != 0u && vload(pool.active) == 0u)) break;
+                if ((nh == 0u || traverse_only) && warp_flag(vload(pool.exhausted) != 0u && vload(pool.active) == 0u))
+                    break;
                 const uint64_t now = wave_timer();
                 if (idle_since == 0) idle_since = now;
                 else if (now - idle_since > kWaitLimitNs) { fail(); break; }
