@@ -26,18 +26,9 @@ namespace orn {
 // Traversal state of one ray, advanced one node per step
 // (bvh.hip.h:145-276 visit order; see trace_ray).  `node` is a typed node
 // reference (pt_scene.h).
-#ifndef ORN_STACK_TOP_REG
-#define ORN_STACK_TOP_REG 1
-#endif
-
 struct Walker {
     uint32_t node;
     int sp;
-    // with ORN_STACK_TOP_REG the stack's top entry (position sp - 1) is kept
-    // here and positions 0..sp-2 in the TravStack: a pop hands over the next
-    // node without waiting for a shared-memory load (the refill of `top`
-    // is only needed at the following pop)
-    uint32_t top;
     int blas_sp;
     bool in_blas;
     bool any;
@@ -58,7 +49,6 @@ struct Walker {
 __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 ro, f3 rd) {
     w.node = sc.root_ref;
     w.sp = 0;
-    w.top = 0;
     w.blas_sp = 0;
     w.in_blas = false;
     w.any = false;
@@ -108,13 +98,7 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
             have_next = true;
             if (hl) {
                 if (w.sp >= kStackSize) { *err |= ERR_STACK; w.any = false; return false; }
-#if ORN_STACK_TOP_REG
-                if (w.sp > 0) stack.put(w.sp - 1, w.top);
-                w.top = lref;
-                ++w.sp;
-#else
                 stack.put(w.sp++, lref);
-#endif
             }
         } else if (hl) {
             next = lref;
@@ -209,12 +193,7 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
             if (COUNT) vc->visits += w.visits;
             return false;
         }
-#if ORN_STACK_TOP_REG
-        next = w.top;
-        if (--w.sp > 0) w.top = stack.get(w.sp - 1);
-#else
         next = stack.get(--w.sp);
-#endif
     }
     w.node = next;
     return true;
