@@ -211,8 +211,14 @@ wave_kernel(RenderLaunch p) {
         }
         return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
     };
-    wave_warp<COUNT, FAST, false, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
-                                     (threadIdx.x >> 5) < (uint32_t)NS ? ROLE_SHADE : ROLE_TRAVERSE, shade);
+    const uint32_t warp = threadIdx.x >> 5;
+    if (warp >= (uint32_t)NS) {
+        // traversal warps: their lanes' stacks are the first 32 * (NW - NS)
+        // columns of the shared stack array
+        traversal_warp<COUNT, FAST, P>(pool, p, sstack + (threadIdx.x - 32 * NS), 32 * (NW - NS), lane, vc, err);
+    } else {
+        wave_warp<COUNT, FAST, false, P, ROLE_SHADE>(pool, p, sstack, 32 * (NW - NS), lane, vc, err, shade);
+    }
 
     if (err) atomicOr(p.error, err);
     if (COUNT) {
@@ -239,7 +245,7 @@ namespace {
 #define ORN_WAVE_WARPS 8
 #endif
 #ifndef ORN_WAVE_SLOTS
-#define ORN_WAVE_SLOTS 320
+#define ORN_WAVE_SLOTS 256
 #endif
 // warps of a block that shade (the others traverse)
 #ifndef ORN_WAVE_SHADERS
@@ -250,7 +256,8 @@ constexpr int kWaveW = ORN_WAVE_WARPS, kWaveP = ORN_WAVE_SLOTS, kWaveS = ORN_WAV
 template <int SEM, bool COUNT, bool FAST>
 cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
     constexpr int kBlock = 32 * kWaveW;
-    constexpr size_t kSmem = ((sizeof(Pool<kWaveP>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * kBlock;
+    constexpr size_t kSmem =
+        ((sizeof(Pool<kWaveP>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * 32 * (kWaveW - kWaveS);
     static int blocks_per_sm = 0, sms = 0;
     auto kern = wave_kernel<SEM, COUNT, FAST, kWaveW, kWaveS, kWaveP>;
     // more than 48 KB of dynamic shared memory: an opt-in per device

@@ -474,8 +474,12 @@ wave_cached_kernel(RenderLaunch p) {
         }
         return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
     };
-    wave_warp<false, FAST, true, P>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
-                                    (threadIdx.x >> 5) < (uint32_t)NS ? ROLE_SHADE : ROLE_BOTH, shade);
+    if ((threadIdx.x >> 5) < (uint32_t)NS)
+        wave_warp<false, FAST, true, P, ROLE_SHADE>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
+                                                    shade);
+    else
+        wave_warp<false, FAST, true, P, ROLE_BOTH>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
+                                                   shade);
     if (err) atomicOr(p.error, err);
 }
 
