@@ -277,25 +277,33 @@ def cpu_baseline(bvh, scene, args, seconds, threads=0):
     return value, nthreads, f"every {stride}th pixel of the frame ({pixels} pixels) x {spp} spp, {dt:.1f} s"
 
 
-def source_hash():
-    """Hash of the kernel sources and build flags (csrc/, include/, build.py):
-    identifies the build an ncu capture was taken of."""
+def source_hash(files=None):
+    """Hash of kernel sources and the build flags: `files` (paths relative to
+    the repository: the translation units and headers of one kernel and its
+    host launcher), or every file of csrc/ and include/ plus build.py.
+    Identifies the build an ncu capture was taken of."""
     import hashlib
     h = hashlib.sha256()
-    files = (sorted((ROOT / "zig_ornament_gb300" / "csrc").glob("*")) + sorted((ROOT / "include").glob("*.h"))
-             + [ROOT / "zig_ornament_gb300" / "build.py"])
-    for f in files:
+    if files is None:
+        paths = (sorted((ROOT / "zig_ornament_gb300" / "csrc").glob("*")) + sorted((ROOT / "include").glob("*.h"))
+                 + [ROOT / "zig_ornament_gb300" / "build.py"])
+    else:
+        paths = [ROOT / f for f in files]
+    for f in paths:
         if f.is_file():
             h.update(f.name.encode())
             h.update(f.read_bytes())
+        else:
+            h.update(b"missing:" + str(f.name).encode())
     return h.hexdigest()[:16]
 
 
 def profile_figures(name):
     """(figures, source) of a committed ncu summary, profiles/<name>.md, whose
     `figures:` line holds the counters bench.py quotes (DRAM bytes per node
-    visit, SOL percentages); figures is None unless that capture was taken
-    of the current kernel sources (source_hash)."""
+    visit, SOL percentages) and the source files the captured kernel was
+    built from; figures is None unless those files are unchanged since the
+    capture (source_hash)."""
     p = ROOT / "profiles" / f"{name}.md"
     if not p.exists():
         return None, f"profiles/{name}.md absent"
@@ -305,10 +313,16 @@ def profile_figures(name):
                 d = json.loads(line.split(":", 1)[1])
             except ValueError:
                 return None, f"profiles/{name}.md: unreadable figures line"
-            if d.get("sources") != source_hash():
+            if d.get("sources") != source_hash(d.get("files")):
                 return None, f"profiles/{name}.md was captured from other kernel sources"
             return d, f"profiles/{name}.md (ncu, this build)"
     return None, f"profiles/{name}.md has no figures line"
+
+
+# The sources of the megakernel and its launcher (profile figures lines).
+MEGA_SOURCES = ["zig_ornament_gb300/csrc/" + f for f in (
+    "megakernel.cu", "pt_device.cuh", "pt_machine.cuh", "pt_kernels.h", "pt_scene.h", "pmath.h", "qmc.cuh",
+    "capi.cu", "order.cu")] + ["include/ornament_cuda.h", "zig_ornament_gb300/build.py"]
 
 
 def l1_peak_gbs(clocks, device=0):

@@ -51,6 +51,7 @@ def test_profile_figures_only_for_the_current_build(tmp_path, monkeypatch):
     import bench
     h = bench.source_hash()
     assert h == bench.source_hash() and len(h) == 16
+    assert bench.source_hash(bench.MEGA_SOURCES) != h
     prof = tmp_path / "profiles"
     prof.mkdir()
     fig = {"sources": h, "dram_bytes_per_visit": 1.5, "l1tex_pct": 60.0}
@@ -58,7 +59,7 @@ def test_profile_figures_only_for_the_current_build(tmp_path, monkeypatch):
     (prof / "k_old.md").write_text("figures: " + json.dumps(dict(fig, sources="0" * 16)) + "\n")
     (prof / "k_none.md").write_text("# no figures\n")
     monkeypatch.setattr(bench, "ROOT", tmp_path)
-    monkeypatch.setattr(bench, "source_hash", lambda: h)
+    monkeypatch.setattr(bench, "source_hash", lambda files=None: h)
     d, src = bench.profile_figures("k_now")
     assert d["dram_bytes_per_visit"] == 1.5 and "this build" in src
     assert bench.profile_figures("k_old")[0] is None

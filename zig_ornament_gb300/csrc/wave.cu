@@ -217,7 +217,36 @@ wave_kernel(RenderLaunch p) {
         // columns of the shared stack array
         traversal_warp<COUNT, FAST, P>(pool, p, sstack + (threadIdx.x - 32 * NS), 32 * (NW - NS), lane, vc, err);
     } else {
-        wave_warp<COUNT, FAST, false, P, ROLE_SHADE>(pool, p, sstack, 32 * (NW - NS), lane, vc, err, shade);
+        // the shading warp: up to 32 queued hits per round
+        bool ok = true;
+        uint64_t idle_since = 0;
+        for (;;) {
+            if (warp_flag(vload(pool.abort) != 0u)) break;
+            const uint32_t slot = q_pop<P>(pool.hq, &pool.hq_head, &pool.hq_tail, kFull, lane, &ok);
+            if (!__all_sync(kFull, ok)) {
+                pool.abort = 1;
+                err |= ERR_WAIT;
+                break;
+            }
+            if (__ballot_sync(kFull, slot != kEmpty) == 0u) {
+                if (warp_flag(vload(pool.exhausted) != 0u && vload(pool.active) == 0u)) break;
+                const uint64_t now = wave_timer();
+                if (idle_since == 0) idle_since = now;
+                else if (now - idle_since > kWaitLimitNs) {
+                    pool.abort = 1;
+                    err |= ERR_WAIT;
+                    break;
+                }
+                __nanosleep(64);
+                continue;
+            }
+            idle_since = 0;
+            if (!shade(slot)) {
+                pool.abort = 1;
+                err |= ERR_WAIT;
+                break;
+            }
+        }
     }
 
     if (err) atomicOr(p.error, err);
