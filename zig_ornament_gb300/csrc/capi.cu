@@ -312,15 +312,19 @@ void relayout_nodes(const orn_scene_blob* b, std::vector<float4>* out) {
                 o[2] = make_float4(c[0], c[1], c[2], u2f(ORN_NODE_INTERNAL));
                 o[3] = make_float4(e[0], e[1], e[2], 0.0f);
                 break;
-            case ORN_NODE_TRIANGLE:
-                // the vertices as given (the test subtracts them on the fly,
-                // bvh.hip.h:81-82), so triangles sharing an edge see the same
-                // floats (the watertight test relies on it)
+            case ORN_NODE_TRIANGLE: {
+                // the vertices as given, so triangles sharing an edge see the
+                // same floats (the watertight test relies on it), and the two
+                // edges the reference's test subtracts on the fly
+                // (bvh.hip.h:81-82) — the same single-precision subtractions
+                const float e1[3] = {bb[0] - a[0], bb[1] - a[1], bb[2] - a[2]};
+                const float e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
                 o[0] = make_float4(a[0], a[1], a[2], u2f(n.left_or_custom_id));
-                o[1] = make_float4(bb[0], bb[1], bb[2], 0.0f);
-                o[2] = make_float4(c[0], c[1], c[2], u2f(ORN_NODE_TRIANGLE));
-                o[3] = make_float4(0, 0, 0, 0);
+                o[1] = make_float4(bb[0], bb[1], bb[2], e2[0]);
+                o[2] = make_float4(c[0], c[1], c[2], e2[1]);
+                o[3] = make_float4(e1[0], e1[1], e1[2], e2[2]);
                 break;
+            }
             default: {  // sphere / mesh leaf: inverse rows 0..2 inline
                 const float* m = b->transforms + (size_t)n.transform_id * 2 * 16;
                 o[0] = make_float4(m[0], m[1], m[2], m[3]);

@@ -217,15 +217,21 @@ mega_kernel(RenderLaunch p) {
             break;
 
         if (mode == LANE_TRAVERSE) {
+            // a round of up to kStepsPerIteration node visits; the plain kernel
+            // counts them (pixel cost, per-ray visit limit) once per round
+            constexpr bool kPerStep = COUNT || CACHE || F64;
+            uint32_t s = 0;
 #pragma unroll 1
-            for (int s = 0; s < kStepsPerIteration; ++s) {
-                ++steps;
-                if (!walker_step<COUNT, kSmemStack, FAST, CACHE>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon, &h, stack, &vc,
-                                                                 &err)) {
+            while (s < (uint32_t)kStepsPerIteration) {
+                ++s;
+                if (!walker_step<COUNT, kSmemStack, FAST, CACHE, kPerStep>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon,
+                                                                           &h, stack, &vc, &err)) {
                     mode = LANE_SHADE;
                     break;
                 }
             }
+            steps += s;
+            if (!kPerStep && mode == LANE_TRAVERSE && !walker_account_round(w, s, &err)) mode = LANE_SHADE;
         }
 
         const unsigned ready = __ballot_sync(kFull, mode == LANE_SHADE);

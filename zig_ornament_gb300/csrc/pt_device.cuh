@@ -126,7 +126,8 @@ __device__ __forceinline__ f3 safe_invdir(f3 d) {
     float x = fabsf(d.x) > eps ? d.x : (d.x < 0.0f ? -eps : eps);
     float y = fabsf(d.y) > eps ? d.y : (d.y < 0.0f ? -eps : eps);
     float z = fabsf(d.z) > eps ? d.z : (d.z < 0.0f ? -eps : eps);
-    return mk(1.0f / x, 1.0f / y, 1.0f / z);
+    // __frcp_rn: the correctly rounded reciprocal, the same value as 1.0f / x
+    return mk(__frcp_rn(x), __frcp_rn(y), __frcp_rn(z));
 }
 
 __device__ __forceinline__ bool aabb_hit(float4 mn, float4 mx, f3 inv, f3 oxinv, float t_min, float t_max) {
@@ -146,12 +147,32 @@ __device__ __forceinline__ bool aabb_hit(float4 mn, float4 mx, f3 inv, f3 oxinv,
 // 1e30: |invdir| <= 1e5 by construction (safe_invdir), so every product and
 // sum stays finite.  Callers use this form only under that condition
 // (Walker::fast_slabs, SceneDev::exact_slabs).
+#ifndef ORN_MINMAX3
+#define ORN_MINMAX3 1
+#endif
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 __device__ __forceinline__ bool aabb_hit_fast(float4 mn, float4 mx, f3 inv, f3 oxinv, float t_min, float t_max) {
     float fx = mx.x * inv.x + oxinv.x, fy = mx.y * inv.y + oxinv.y, fz = mx.z * inv.z + oxinv.z;
     float nx = mn.x * inv.x + oxinv.x, ny = mn.y * inv.y + oxinv.y, nz = mn.z * inv.z + oxinv.z;
+#if ORN_MINMAX3
+    // three-input minimum / maximum (sm_100+): for NaN-free inputs the same
+    // values as the two-input chains below
+    return max3f(fminf(fx, nx), fminf(fy, ny), fmaxf(fminf(fz, nz), t_min)) <=
+           min3f(fmaxf(fx, nx), fmaxf(fy, ny), fminf(fmaxf(fz, nz), t_max));
+#else
     float max_t = fminf(fminf(fminf(fmaxf(fx, nx), fmaxf(fy, ny)), fmaxf(fz, nz)), t_max);
     float min_t = fmaxf(fmaxf(fmaxf(fminf(fx, nx), fminf(fy, ny)), fminf(fz, nz)), t_min);
     return min_t <= max_t;
+#endif
 }
 
 // A node's 64 bytes (two 256-bit read-only loads), loaded once per visit
@@ -190,6 +211,27 @@ __device__ __forceinline__ bool slab_safe(f3 o) {
 // Möller–Trumbore exactly as bvh.hip.h:72-117 (e1 = v1 - v0, e2 = v2 - v0):
 // true when the hit distance t satisfies t_min <= t < t_max; (u, v) are the
 // weights of v1 and v2.
+// With the edges e1, e2 given (the triangle node stores them, computed with
+// the same single-precision subtractions).
+__device__ __forceinline__ bool tri_mt_edges(f3 o, f3 d, f3 v0, f3 e1, f3 e2, float t_min, float t_max,
+                                             float* t_out, float* u_out, float* v_out) {
+    const f3 s1 = cross(d, e2);
+    const float det = dot(s1, e1);
+    const float invd = __frcp_rn(det);   // correctly rounded, as 1.0f / det
+    const f3 dd = sub(o, v0);
+    const float u = dot(dd, s1) * invd;
+    if (u < 0.0f || u > 1.0f) return false;
+    const f3 s2 = cross(dd, e1);
+    const float v = dot(d, s2) * invd;
+    if (v < 0.0f || u + v > 1.0f) return false;
+    const float t = dot(e2, s2) * invd;
+    if (t < t_min || t > t_max || !(t < t_max)) return false;
+    *t_out = t;
+    *u_out = u;
+    *v_out = v;
+    return true;
+}
+
 __device__ __forceinline__ bool tri_mt(f3 o, f3 d, f3 v0, f3 v1, f3 v2, float t_min, float t_max, float* t_out,
                                        float* u_out, float* v_out) {
     const f3 e1 = sub(v1, v0), e2 = sub(v2, v0);
@@ -344,10 +386,11 @@ __device__ __forceinline__ bool trace_ray(const SceneDev& sc, f3 ro, f3 rd, floa
             }
         } else if (type == ORN_NODE_TRIANGLE) {
             if (COUNT) vc->tri++;
-            const f3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+            const f3 v0 = mk(a.x, a.y, a.z);
             float t, u, v;
-            const bool hit = sc.watertight ? tri_watertight(o, d, v0, v1, v2, t_min, t_max, &t, &u, &v)
-                                           : tri_mt(o, d, v0, v1, v2, t_min, t_max, &t, &u, &v);
+            const bool hit = sc.watertight
+                                 ? tri_watertight(o, d, v0, mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), t_min, t_max, &t, &u, &v)
+                                 : tri_mt_edges(o, d, v0, mk(e.x, e.y, e.z), mk(b.w, c.w, e.w), t_min, t_max, &t, &u, &v);
             if (hit) {
                 any = true;
                 t_max = t;

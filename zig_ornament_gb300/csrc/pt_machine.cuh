@@ -75,11 +75,15 @@ __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 r
 // FAST selects the FMNMX slab test (aabb_hit_fast); the host decides per
 // render whether every ray of the render satisfies its condition
 // (render_fast_slabs in capi.cu).
-template <bool COUNT, int SS, bool FAST, bool ANY = false>
+// CHECK: count the visit and apply the per-ray visit limit here; a caller
+// that passes false counts the visits of a whole round of steps itself
+// (walker_account_round) and the COUNT statistics are then unavailable.
+template <bool COUNT, int SS, bool FAST, bool ANY = false, bool CHECK = true>
 __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro, f3 rd, float t_min,
                                             HitRec* out, TravStack<SS>& stack, VisitCount* vc,
                                             uint32_t* err) {
-    if (++w.visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; w.any = false; return false; }
+    static_assert(CHECK || !COUNT, "visit statistics need the per-step count");
+    if (CHECK && ++w.visits > kMaxVisitsPerRay) { *err |= ERR_VISITS; w.any = false; return false; }
     const uint32_t type = w.node >> 30;
     bool have_next = false;
     uint32_t next = 0;
@@ -106,11 +110,12 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
         }
     } else if (type == ORN_NODE_TRIANGLE) {
         if (COUNT) vc->tri++;
-        const float4 a = nd.a, b = nd.b, c = nd.c;
-        const f3 v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+        const float4 a = nd.a, b = nd.b, c = nd.c, e = nd.e;
+        const f3 v0 = mk(a.x, a.y, a.z);
         float t, u, v;
-        const bool hit = sc.watertight ? tri_watertight(w.o, w.d, v0, v1, v2, t_min, w.t_max, &t, &u, &v)
-                                       : tri_mt(w.o, w.d, v0, v1, v2, t_min, w.t_max, &t, &u, &v);
+        const bool hit = sc.watertight
+                             ? tri_watertight(w.o, w.d, v0, mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), t_min, w.t_max, &t, &u, &v)
+                             : tri_mt_edges(w.o, w.d, v0, mk(e.x, e.y, e.z), mk(b.w, c.w, e.w), t_min, w.t_max, &t, &u, &v);
         if (hit) {
             w.any = true;
             w.t_max = t;
@@ -196,6 +201,19 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
         next = stack.get(--w.sp);
     }
     w.node = next;
+    return true;
+}
+
+// After a round of `steps` walker_step<..., CHECK = false> calls on a ray
+// that is still traversing: counts them and applies the per-ray visit limit
+// (the limit then acts up to one round late); false when the ray is given up.
+__device__ __forceinline__ bool walker_account_round(Walker& w, uint32_t steps, uint32_t* err) {
+    w.visits += steps;
+    if (w.visits > kMaxVisitsPerRay) {
+        *err |= ERR_VISITS;
+        w.any = false;
+        return false;
+    }
     return true;
 }
 

@@ -5,7 +5,8 @@
 // after them with every BLAS id offset by tlas_len), four float4 per node:
 //   internal  a=(left.min, left id)  b=(left.max, right id)
 //             c=(right.min, type=0)  e=(right.max, 0)
-//   triangle  a=(v0, triangle id)    b=(v1, 0)     c=(v2, type=3)  e=0
+//   triangle  a=(v0, triangle id)    b=(v1, e2.x)  c=(v2, e2.y)
+//             e=(e1, e2.z)  with e1 = v1 - v0, e2 = v2 - v0
 //   sphere    a,b=inverse rows 0,1   c=(inverse row 2 xyz, type=1)
 //             e=(inverse row 2 w, material, transform id, 0)
 //   mesh      as sphere with type=2 and e.w = BLAS root id
