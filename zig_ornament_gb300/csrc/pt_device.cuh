@@ -147,32 +147,12 @@ __device__ __forceinline__ bool aabb_hit(float4 mn, float4 mx, f3 inv, f3 oxinv,
 // 1e30: |invdir| <= 1e5 by construction (safe_invdir), so every product and
 // sum stays finite.  Callers use this form only under that condition
 // (Walker::fast_slabs, SceneDev::exact_slabs).
-#ifndef ORN_MINMAX3
-#define ORN_MINMAX3 1
-#endif
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-    float r;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-__device__ __forceinline__ float max3f(float a, float b, float c) {
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
 __device__ __forceinline__ bool aabb_hit_fast(float4 mn, float4 mx, f3 inv, f3 oxinv, float t_min, float t_max) {
     float fx = mx.x * inv.x + oxinv.x, fy = mx.y * inv.y + oxinv.y, fz = mx.z * inv.z + oxinv.z;
     float nx = mn.x * inv.x + oxinv.x, ny = mn.y * inv.y + oxinv.y, nz = mn.z * inv.z + oxinv.z;
-#if ORN_MINMAX3
-    // three-input minimum / maximum (sm_100+): for NaN-free inputs the same
-    // values as the two-input chains below
-    return max3f(fminf(fx, nx), fminf(fy, ny), fmaxf(fminf(fz, nz), t_min)) <=
-           min3f(fmaxf(fx, nx), fmaxf(fy, ny), fminf(fmaxf(fz, nz), t_max));
-#else
     float max_t = fminf(fminf(fminf(fmaxf(fx, nx), fmaxf(fy, ny)), fmaxf(fz, nz)), t_max);
     float min_t = fmaxf(fmaxf(fmaxf(fminf(fx, nx), fminf(fy, ny)), fminf(fz, nz)), t_min);
     return min_t <= max_t;
-#endif
 }
 
 // A node's 64 bytes (two 256-bit read-only loads), loaded once per visit
