@@ -166,13 +166,6 @@ constexpr int kCacheShadeThreshold = ORN_CACHE_SHADE_THRESHOLD;
 #define ORN_STEPS_PER_ITERATION 32
 #endif
 constexpr int kStepsPerIteration = ORN_STEPS_PER_ITERATION;
-// steps between the megakernel's checks for enough lanes waiting to be
-// shaded within a round (a divisor of kStepsPerIteration)
-#ifndef ORN_ROUND_CHUNK
-#define ORN_ROUND_CHUNK 8
-#endif
-constexpr int kRoundChunk = ORN_ROUND_CHUNK;
-static_assert(kStepsPerIteration % kRoundChunk == 0, "round chunks must divide the round");
 
 
 // Arguments of one wavefront iteration (wavefront.cu).  Path slots are
