@@ -33,9 +33,6 @@ struct Walker {
     bool in_blas;
     bool any;
     f3 o, d, inv, oxinv;
-#ifndef ORN_RECOMPUTE_WORLD_INV
-    f3 winv, woxinv;   // world-space values, restored on BLAS exit
-#endif
     float t_max;
     uint32_t material, inv_id;
     uint32_t visits;
@@ -58,10 +55,6 @@ __device__ __forceinline__ void walker_begin(Walker& w, const SceneDev& sc, f3 r
     w.d = rd;
     w.inv = safe_invdir(rd);
     w.oxinv = mul(neg(ro), w.inv);
-#ifndef ORN_RECOMPUTE_WORLD_INV
-    w.winv = w.inv;
-    w.woxinv = w.oxinv;
-#endif
     w.t_max = (float)3.40282e+38;
     w.material = 0;
     w.inv_id = 0;
@@ -186,13 +179,10 @@ __device__ __forceinline__ bool walker_step(Walker& w, const SceneDev& sc, f3 ro
             w.in_blas = false;
             w.o = ro;
             w.d = rd;
-#ifdef ORN_RECOMPUTE_WORLD_INV
+            // recomputed rather than kept: six registers fewer for every
+            // step (measured +0.8 % on the 1080p step)
             w.inv = safe_invdir(rd);
             w.oxinv = mul(neg(ro), w.inv);
-#else
-            w.inv = w.winv;
-            w.oxinv = w.woxinv;
-#endif
         }
         if (w.sp == 0) {
             if (COUNT) vc->visits += w.visits;
