@@ -300,16 +300,21 @@ __device__ __forceinline__ void traversal_warp(Pool& pool, const RenderLaunch& p
         bool fin = false;
         uint32_t flag = HIT_MISS;
         if (slot != kEmpty) {
+            // visits counted once per round, as in the megakernel
+            uint32_t s = 0;
+            const uint32_t e0 = err;
 #pragma unroll 1
-            for (int s = 0; s < kWaveSteps; ++s) {
-                ++steps;
-                const uint32_t e0 = err;
-                if (!walker_step<COUNT, kSmemStack, FAST>(w, p.scene, ro, rd, t_min, &h, stack, &vc, &err)) {
+            while (s < (uint32_t)kWaveSteps) {
+                ++s;
+                if (!walker_step<COUNT, kSmemStack, FAST, false, COUNT>(w, p.scene, ro, rd, t_min, &h, stack, &vc,
+                                                                        &err)) {
                     fin = true;
-                    flag = err != e0 ? HIT_FAILED : (w.any ? HIT_ANY : HIT_MISS);
                     break;
                 }
             }
+            steps += s;
+            if (!COUNT && !fin && !walker_account_round(w, s, &err)) fin = true;
+            if (fin) flag = err != e0 ? HIT_FAILED : (w.any ? HIT_ANY : HIT_MISS);
         }
         if (fin) {
             pool.t[slot] = h.t;
