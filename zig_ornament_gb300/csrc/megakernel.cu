@@ -68,10 +68,6 @@ template <> struct Accum<true> {
 // first rough surface from the second vertex on) and leaves a query there; a
 // training pixel's path runs to the end and records the network inputs at
 // the cache vertex and the radiance that left it.
-#ifndef ORN_STEP_UNROLL
-#define ORN_STEP_UNROLL 1
-#endif
-constexpr int kStepUnroll = ORN_STEP_UNROLL;   // unroll factor of the traversal round
 #ifndef ORN_CACHE_MIN_BLOCKS
 #define ORN_CACHE_MIN_BLOCKS 4
 #endif
@@ -228,7 +224,7 @@ mega_kernel(RenderLaunch p) {
             // slower: the extra ballots cost more than the waiting lanes.)
             constexpr bool kPerStep = COUNT || CACHE || F64;
             uint32_t s = 0;
-#pragma unroll (kStepUnroll)
+#pragma unroll 1
             while (s < (uint32_t)kStepsPerIteration) {
                 ++s;
                 if (!walker_step<COUNT, kSmemStack, FAST, CACHE, kPerStep>(w, p.scene, ro, rd, p.cp.ray_cast_epsilon,
