@@ -37,14 +37,17 @@ of the frame (replicas: pixels and samples are independent, no exchange);
 value = all ranks' samples / the slowest rank's time.
 
 The headline line also carries: the same steps on the non-parity trees
-(`sah_tree`, `lbvh_tree`); `configs` — the sphere field (640x360, 64 spp),
+(`sah_tree`, `lbvh_tree`); the same steps on the persistent wavefront with
+its autotuned launch parameters (`wavefront`, same images);
+`configs` — the sphere field (640x360, 64 spp),
 the large scene (3840x2160, 16 spp, depth 16) and the 64-scene batch (every
 scene's full sample count, one graph-replayed launch against one launch per
 scene), each with rays/s, roofline and CPU baseline; and `time_to_relmse` —
 plain tracing on the parity and SAH trees against the cached renderers, to
 relMSE 1e-3 against a 16k-sample FP64 oracle, on the radiance-cache
 configuration at 1920x1080 and a closed room at 640x360.  Other modes:
-`--workload spheres|large`, `--bvh sah|lbvh`, `--kernel wavefront`,
+`--workload spheres|large`, `--bvh sah|lbvh`, `--kernel wavefront` (after
+orn_wave_tune unless `--no-wave-tune`),
 `--mode relmse` (the block alone; `--workload large` for the large scene at
 960x540), `--mode batch`, `--mode cached-frames [--batched]` (a profiling
 workload of radiance-cache frames).
@@ -105,6 +108,10 @@ def parse():
     p.add_argument("--tune-cache", default=None, help="batch: autotuner JSON cache (default: none)")
     p.add_argument("--no-relmse", action="store_true", help="skip the time-to-relMSE block")
     p.add_argument("--no-sah-line", action="store_true", help="skip the SAH-tree figure")
+    p.add_argument("--no-wavefront-line", action="store_true",
+                   help="skip the persistent wavefront's figure in the headline line")
+    p.add_argument("--no-wave-tune", action="store_true",
+                   help="--kernel wavefront: keep the default launch parameters instead of orn_wave_tune's")
     p.add_argument("--no-configs", action="store_true",
                    help="skip the other configurations (sphere field, 64-scene batch, large scene)")
     p.add_argument("--relmse-width", type=int, default=1920)
@@ -430,6 +437,12 @@ def run_ours(args):
     st.kernel = _lib.KERNEL_WAVEFRONT if args.kernel == "wavefront" else _lib.KERNEL_MEGA
     r.set_state(st)
     r.set_camera(scene.camera.to_struct())
+    if args.kernel == "wavefront":
+        # the autotuner picks the block shape, fetch threshold and round
+        # length for this scene and resolution (untimed; scratch targets)
+        t_tune = time.perf_counter()
+        wave_cfg = r.wave_config() if args.no_wave_tune else r.wave_tune()
+        cfg["wave_config"] = {**wave_cfg, "tune_s": round(time.perf_counter() - t_tune, 2)}
     stream = torch.cuda.ExternalStream(r.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     n_px = args.width * args.height
@@ -529,6 +542,19 @@ def run_ours(args):
                                      "reference's in expectation only"}
             except Exception as exc:
                 line[key] = {"error": f"{type(exc).__name__}: {exc}"}
+    if headline and not args.no_wavefront_line:
+        # the same steps on the persistent wavefront (same images), with the
+        # launch parameters its autotuner picks for this workload
+        try:
+            m = measure_megakernel(bvh, scene, args.width, args.height, args.spp, args.depth, args.steps,
+                                   args.warmup, local, flush, kernel="wavefront")
+            line["wavefront"] = {"value": m["value"], "unit": UNIT, "vs_megakernel": m["value"] / value,
+                                 "ms_per_step": m["ms_per_step"], "launches_per_step": m["launches_per_step"],
+                                 "wave_config": m["wave_config"],
+                                 "note": "persistent wavefront (ORN_KERNEL_WAVEFRONT), bit-identical images; "
+                                         "device time of the same renders, L2 flushed between them"}
+        except Exception as exc:
+            line["wavefront"] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.no_cpu_baseline:
         v, cores, desc = cpu_baseline(bvh, scene, args, args.cpu_seconds)
         v1, _, desc1 = cpu_baseline(bvh, scene, args, 4.0, threads=1)
@@ -570,10 +596,12 @@ def port_speed_note():
     return note
 
 
-def measure_megakernel(bvh, scene, w, h, spp, depth, steps, warmup, local, flush, counters=False):
+def measure_megakernel(bvh, scene, w, h, spp, depth, steps, warmup, local, flush, counters=False, kernel="mega"):
     """Device time of `steps` renders of `spp` passes (L2 flushed between
     them); returns Msamples/s, ms per step, launches per step and, with
-    `counters`, the exact work of one more (untimed) render."""
+    `counters`, the exact work of one more (untimed) render.  kernel
+    "wavefront" renders on the persistent wavefront with the launch
+    parameters orn_wave_tune picks (untimed; returned as wave_config)."""
     import torch
     from zig_ornament_gb300 import _lib, ornament
     r = ornament.Renderer(bvh, device=local)
@@ -581,9 +609,13 @@ def measure_megakernel(bvh, scene, w, h, spp, depth, steps, warmup, local, flush
     st = _lib.State()
     st.depth, st.flip_y, st.inverted_gamma, st.iterations = depth, 0, 1.0, spp
     st.ray_cast_epsilon, st.semantics, st.spp_per_launch = 0.001, 0, 0
-    st.kernel = _lib.KERNEL_MEGA
+    st.kernel = _lib.KERNEL_WAVEFRONT if kernel == "wavefront" else _lib.KERNEL_MEGA
     r.set_state(st)
     r.set_camera(scene.camera.to_struct())
+    wave_cfg = None
+    if kernel == "wavefront":
+        t_tune = time.perf_counter()
+        wave_cfg = {**r.wave_tune(), "tune_s": round(time.perf_counter() - t_tune, 2)}
     stream = torch.cuda.ExternalStream(r.stream(), device=torch.device("cuda", local))
 
     def flush_l2():
@@ -604,6 +636,8 @@ def measure_megakernel(bvh, scene, w, h, spp, depth, steps, warmup, local, flush
     launches = (r.launch_count() - l0) / steps
     out = {"value": w * h * spp / (float(np.mean(ms)) / 1e3) / 1e6, "ms_per_step": float(np.mean(ms)),
            "launches_per_step": launches}
+    if wave_cfg is not None:
+        out["wave_config"] = wave_cfg
     if counters:
         r.enable_counters(True)
         r.render()

@@ -274,6 +274,34 @@ int orn_render(orn_context* ctx);
 /* Blocks until all work queued on the context has finished. */
 int orn_synchronize(orn_context* ctx);
 
+/* Launch parameters of ORN_KERNEL_WAVEFRONT (no counterpart in the
+ * reference, whose launch shape is fixed by its grid).  Every configuration
+ * renders the same bits; only the speed differs.  Counting renders
+ * (orn_enable_counters) always run shape 0. */
+typedef struct orn_wave_config {
+    uint32_t shape;   /* block shape: 0 = 10 warps (9 traversing, 1 shading),
+                         320 path slots, 2 blocks per SM (default);
+                         1 = 8 warps (7 + 1), 256 slots, 3 blocks per SM;
+                         2 = 12 warps (11 + 1), 384 slots, 2 blocks per SM;
+                         3 = 11 warps (10 + 1), 352 slots, 2 blocks per SM */
+    uint32_t fetch;   /* idle lanes a traversing warp gathers before it takes
+                         new rays: 1..32 (default 4) */
+    uint32_t steps;   /* node visits per traversal round: 4..256 (default 32) */
+    uint32_t tuned;   /* out: 1 when chosen by orn_wave_tune */
+} orn_wave_config;
+int orn_wave_get_config(const orn_context* ctx, orn_wave_config* out);
+/* ORN_ERR_INVALID_ARGUMENT outside the ranges above. */
+int orn_wave_set_config(orn_context* ctx, orn_wave_config const* config);
+/* Autotuner: renders one launch (the passes orn_render would put in one
+ * launch, at most 8) of the context's current scene, camera, resolution and
+ * state with every candidate (4 shapes x fetch 2/4/8 x steps 32/64) into
+ * scratch targets — the context's image, RNG states and pixel order are not
+ * touched — and keeps the fastest.  With `cache_path`, a JSON file keyed by
+ * device and workload (pixels, passes, depth, semantics, tree sizes) is
+ * read first and updated after tuning.  `chosen` may be NULL.
+ * Synchronous. */
+int orn_wave_tune(orn_context* ctx, const char* cache_path, orn_wave_config* chosen);
+
 /* PathTracer.getFrameBuffer — src/hip_backend/path_tracer.zig:111-119.
  * `dst` holds pixel_count RGBA float4 values (16 bytes each). */
 int orn_get_framebuffer(orn_context* ctx, float* dst, size_t pixel_count);
@@ -344,11 +372,13 @@ int orn_relmse(orn_context* ctx, const double* reference_mean_rgba, size_t pixel
 /* One-tile tensor-core GEMM self-test (no counterpart in the reference):
  * D[128 x N] = A[128 x K] · B[N x K]^T with 16-bit A, B (F16, or BF16 when
  * `bf16`), row-major host arrays, FP32 result.  K a multiple of 16 up to
- * 256, N a multiple of 16 from 16 to 128.  `swap_offsets` exchanges the two
- * operand-descriptor byte offsets (a deliberately wrong encoding, to show
- * the test can tell them apart).  Checks the tcgen05 encodings the radiance
- * cache relies on.  Synchronous; uses device 0. */
-int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int swap_offsets, const uint16_t* A, const uint16_t* B,
+ * 256, N a multiple of 16 from 16 to 128.  `mode` bit 1 stages both
+ * operands MN-major instead of K-major (the layout of the weight-gradient
+ * GEMMs); bit 0 exchanges the two operand-descriptor byte offsets (a
+ * deliberately wrong encoding, to show the test can tell them apart).
+ * Checks the tcgen05 encodings the radiance cache relies on.  Synchronous;
+ * uses device 0. */
+int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int mode, const uint16_t* A, const uint16_t* B,
                     float* D);
 
 /* ---- rendering without allocation -----------------------------------------

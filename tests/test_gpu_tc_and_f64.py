@@ -21,22 +21,24 @@ def to16(x, bf16):
     return h.view(np.uint16), h.astype(np.float32)
 
 
+@pytest.mark.parametrize("mn_major", [False, True])
 @pytest.mark.parametrize("bf16", [False, True])
-@pytest.mark.parametrize("K,N", [(16, 16), (64, 64), (256, 64), (64, 128), (256, 16)])
-def test_tcgen05_gemm_matches_host(K, N, bf16):
+@pytest.mark.parametrize("K,N", [(16, 16), (64, 64), (256, 64), (64, 128), (256, 16), (128, 64), (128, 16)])
+def test_tcgen05_gemm_matches_host(K, N, bf16, mn_major):
     lib = _lib.load()
     rs = np.random.default_rng(K * 1000 + N + bf16)
     a16, a = to16(rs.normal(size=(128, K)), bf16)
     b16, b = to16(rs.normal(size=(N, K)), bf16)
     d = np.zeros((128, N), np.float32)
-    st = lib.orn_tc_selftest(K, N, int(bf16), 0, a16.ctypes.data, b16.ctypes.data, d.ctypes.data)
+    mode = 2 if mn_major else 0
+    st = lib.orn_tc_selftest(K, N, int(bf16), mode, a16.ctypes.data, b16.ctypes.data, d.ctypes.data)
     assert st == 0, lib.orn_status_string(st)
     ref = a.astype(np.float64) @ b.astype(np.float64).T
     assert np.allclose(d, ref, rtol=1e-4, atol=1e-3 * np.sqrt(K)), np.abs(d - ref).max()
     if K > 16:
         # exchanging the two descriptor offsets reads the operands in a different order
         d2 = np.zeros_like(d)
-        assert lib.orn_tc_selftest(K, N, int(bf16), 1, a16.ctypes.data, b16.ctypes.data, d2.ctypes.data) == 0
+        assert lib.orn_tc_selftest(K, N, int(bf16), mode | 1, a16.ctypes.data, b16.ctypes.data, d2.ctypes.data) == 0
         assert not np.allclose(d2, ref, rtol=1e-4, atol=1e-3 * np.sqrt(K))
 
 

@@ -161,6 +161,10 @@ class BatchConfig(C.Structure):
                 ("tuned", C.c_uint32)]
 
 
+class WaveConfig(C.Structure):
+    _fields_ = [("shape", C.c_uint32), ("fetch", C.c_uint32), ("steps", C.c_uint32), ("tuned", C.c_uint32)]
+
+
 _P = C.c_void_p
 FUNCTIONS = {
     "orn_create": (C.c_int, [_P, C.c_int, C.POINTER(C.c_void_p)]),
@@ -208,6 +212,9 @@ FUNCTIONS = {
     "orn_batch_get_config": (C.c_int, [_P, C.POINTER(BatchConfig)]),
     "orn_batch_set_config": (C.c_int, [_P, C.POINTER(BatchConfig)]),
     "orn_batch_tune": (C.c_int, [_P, C.c_char_p, C.POINTER(BatchConfig)]),
+    "orn_wave_get_config": (C.c_int, [_P, C.POINTER(WaveConfig)]),
+    "orn_wave_set_config": (C.c_int, [_P, C.POINTER(WaveConfig)]),
+    "orn_wave_tune": (C.c_int, [_P, C.c_char_p, C.POINTER(WaveConfig)]),
     "orn_batch_last_error": (C.c_char_p, [_P]),
     "orn_last_error": (C.c_char_p, [_P]),
     "orn_status_string": (C.c_char_p, [C.c_int]),

@@ -29,6 +29,7 @@
 #include "pt_kernels.h"
 #include "pt_device.cuh"
 #include "pt_machine.cuh"
+#include "tune_cache.h"
 
 namespace orn {
 
@@ -360,66 +361,19 @@ bool valid_config(int block, int blocks_per_sm, int shade_threshold) {
            shade_threshold >= 1 && shade_threshold <= 32;
 }
 
+// The file's entries that hold a launchable configuration (one outside the
+// range, from a hand-edited or foreign file, is dropped: its workload is
+// tuned again).
 std::map<std::string, orn::BatchConfig> read_cache(const char* path) {
     std::map<std::string, orn::BatchConfig> out;
-    if (!path) return out;
-    FILE* f = std::fopen(path, "rb");
-    if (!f) return out;
-    std::string s;
-    char buf[4096];
-    size_t n;
-    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, n);
-    std::fclose(f);
-    size_t pos = 0;
-    auto num = [&](const std::string& obj, const char* name, int* v) {
-        size_t p = obj.find(std::string("\"") + name + "\"");
-        if (p == std::string::npos) return false;
-        p = obj.find(':', p);
-        if (p == std::string::npos) return false;
-        *v = (int)std::strtol(obj.c_str() + p + 1, nullptr, 10);
-        return true;
-    };
-    while ((pos = s.find('"', pos)) != std::string::npos) {
-        const size_t kend = s.find('"', pos + 1);
-        if (kend == std::string::npos) break;
-        const std::string key = s.substr(pos + 1, kend - pos - 1);
-        const size_t ob = s.find_first_not_of(" \t\r\n:", kend + 1);
-        if (ob == std::string::npos || s[ob] != '{') {
-            pos = kend + 1;
-            continue;
-        }
-        const size_t cb = s.find('}', ob);
-        if (cb == std::string::npos) break;
-        const std::string obj = s.substr(ob, cb - ob + 1);
-        orn::BatchConfig c{};
-        // an entry outside the launchable range (a hand-edited or foreign
-        // file) is dropped: its workload is tuned again
-        if (num(obj, "block", &c.block) && num(obj, "blocks_per_sm", &c.blocks_per_sm) &&
-            num(obj, "shade_threshold", &c.shade_threshold) &&
-            valid_config(c.block, c.blocks_per_sm, c.shade_threshold))
-            out[key] = c;
-        pos = cb + 1;
+    for (const auto& kv : orn::read_tune_cache(path)) {
+        const auto& f = kv.second.fields;
+        auto b = f.find("block"), n = f.find("blocks_per_sm"), t = f.find("shade_threshold");
+        if (b == f.end() || n == f.end() || t == f.end()) continue;
+        orn::BatchConfig c{(int)b->second, (int)n->second, (int)t->second};
+        if (valid_config(c.block, c.blocks_per_sm, c.shade_threshold)) out[kv.first] = c;
     }
     return out;
-}
-
-bool write_cache(const char* path, const std::map<std::string, orn::BatchConfig>& m,
-                 const std::map<std::string, float>& ms) {
-    if (!path) return false;
-    const std::string tmp = std::string(path) + ".tmp";
-    FILE* f = std::fopen(tmp.c_str(), "wb");
-    if (!f) return false;
-    std::fprintf(f, "{\n");
-    size_t i = 0;
-    for (const auto& kv : m) {
-        auto t = ms.find(kv.first);
-        std::fprintf(f, "  \"%s\": {\"block\": %d, \"blocks_per_sm\": %d, \"shade_threshold\": %d, \"ms\": %.3f}%s\n",
-                     kv.first.c_str(), kv.second.block, kv.second.blocks_per_sm, kv.second.shade_threshold,
-                     t == ms.end() ? 0.0f : t->second, ++i < m.size() ? "," : "");
-    }
-    std::fprintf(f, "}\n");
-    std::fclose(f);
-    return std::rename(tmp.c_str(), path) == 0;
 }
 
 }  // namespace
@@ -650,10 +604,14 @@ int orn_batch_tune(orn_batch* b, const char* cache_path, orn_batch_config* chose
     b->config = best;
     b->tuned = true;
     if (cache_path) {
-        cache[key] = best;
-        std::map<std::string, float> ms;
-        ms[key] = best_ms;
-        write_cache(cache_path, cache, ms);
+        auto entries = orn::read_tune_cache(cache_path);
+        orn::TuneEntry e;
+        e.fields["block"] = best.block;
+        e.fields["blocks_per_sm"] = best.blocks_per_sm;
+        e.fields["shade_threshold"] = best.shade_threshold;
+        e.ms = best_ms;
+        entries[key] = e;
+        orn::write_tune_cache(cache_path, entries, {"block", "blocks_per_sm", "shade_threshold"});
     }
     if (chosen) orn_batch_get_config(b, chosen);
     return ORN_OK;

@@ -26,6 +26,7 @@
 #include "pt_kernels.h"
 #include "batch.h"
 #include "rc_host.h"
+#include "tune_cache.h"
 
 using orn::RenderLaunch;
 using orn::SceneDev;
@@ -96,6 +97,10 @@ struct orn_context {
     const float4* d_lights = nullptr;
     const float* d_light_cdf = nullptr;
     const uint32_t* d_light_material = nullptr;
+    // launch parameters of the persistent wavefront (ORN_KERNEL_WAVEFRONT),
+    // set by orn_wave_set_config or orn_wave_tune
+    orn::WaveConfig wave_cfg = orn::kWaveDefault;
+    bool wave_tuned = false;
 };
 
 namespace {
@@ -536,6 +541,8 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     p.do_post = 0;
     p.spp = 1;
     p.shade_threshold = orn::kCacheShadeThreshold;
+    p.wave_fetch = orn::kWaveFetchDefault;
+    p.wave_steps = orn::kWaveStepsDefault;
     const uint32_t streams = ctx->cq_streams;
     p.cache.streams = streams;
     p.cache.rng_extra = ctx->rng_extra;
@@ -985,6 +992,8 @@ int orn_render(orn_context* ctx) {
     p.counters = ctx->d_counters;
     p.work_counter = ctx->d_work;
     p.shade_threshold = orn::kShadeThreshold;
+    p.wave_fetch = ctx->wave_cfg.fetch;
+    p.wave_steps = ctx->wave_cfg.steps;
     if (ctx->counters_enabled)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long), ctx->stream));
     if (is_cached(ctx)) {
@@ -1007,7 +1016,7 @@ int orn_render(orn_context* ctx) {
         p.do_post = (done + n == passes) ? 1u : 0u;
         use_pixel_order(ctx, &p);
         if (ctx->state.kernel == ORN_KERNEL_WAVEFRONT) {
-            ORN_CUDA(ctx, orn::launch_wave(p, (int)ctx->state.semantics, ctx->counters_enabled,
+            ORN_CUDA(ctx, orn::launch_wave(p, ctx->wave_cfg, (int)ctx->state.semantics, ctx->counters_enabled,
                                            render_fast_slabs(ctx), ctx->stream));
         } else {
             ORN_CUDA(ctx, orn::launch_mega(p, (int)ctx->state.semantics, orn::MATH_PORTABLE,
@@ -1228,6 +1237,160 @@ int orn_get_counters(orn_context* ctx, uint64_t* out, size_t count) {
     unsigned long long tmp[ORN_COUNTER_COUNT];
     ORN_CUDA(ctx, cudaMemcpy(tmp, ctx->d_counters, sizeof(tmp), cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < count && i < ORN_COUNTER_COUNT; ++i) out[i] = tmp[i];
+    return ORN_OK;
+}
+
+}  // extern "C"
+
+// ---- persistent-wavefront launch parameters and their autotuner ------------------
+extern "C" {
+
+int orn_wave_get_config(const orn_context* ctx, orn_wave_config* out) {
+    if (!ctx || !out) return ORN_ERR_INVALID_ARGUMENT;
+    out->shape = (uint32_t)ctx->wave_cfg.shape;
+    out->fetch = (uint32_t)ctx->wave_cfg.fetch;
+    out->steps = (uint32_t)ctx->wave_cfg.steps;
+    out->tuned = ctx->wave_tuned ? 1u : 0u;
+    return ORN_OK;
+}
+
+int orn_wave_set_config(orn_context* ctx, const orn_wave_config* c) {
+    if (!ctx || !c) return ORN_ERR_INVALID_ARGUMENT;
+    if (c->shape >= (uint32_t)orn::kWaveShapes || c->fetch > 32u || c->steps > 256u ||
+        !orn::wave_config_valid((int)c->shape, (int)c->fetch, (int)c->steps))
+        return fail(ctx, ORN_ERR_INVALID_ARGUMENT,
+                    "invalid wavefront configuration (shape 0..3, fetch 1..32, steps 4..256)");
+    ctx->wave_cfg = orn::WaveConfig{(int)c->shape, (int)c->fetch, (int)c->steps};
+    ctx->wave_tuned = false;
+    return ORN_OK;
+}
+
+int orn_wave_tune(orn_context* ctx, const char* cache_path, orn_wave_config* chosen) {
+    if (!ctx) return ORN_ERR_INVALID_ARGUMENT;
+    if (!ctx->camera_set) return fail(ctx, ORN_ERR_INVALID_ARGUMENT, "no camera set (orn_set_camera)");
+    ORN_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = ensure_target(ctx);
+    if (st) return st;
+    st = sync_and_check(ctx);
+    if (st) return st;
+    const uint32_t n = ctx->width * ctx->height;
+    // the passes of one launch as orn_render would issue them, at most 8
+    const uint32_t passes = std::max<uint32_t>(ctx->state.iterations, 1u);
+    uint32_t chunk = ctx->state.spp_per_launch;
+    if (chunk == 0) chunk = passes <= 64 ? passes : 32;
+    const uint32_t tune_spp = std::min<uint32_t>(chunk, 8u);
+    const bool fast = render_fast_slabs(ctx);
+    cudaDeviceProp prop;
+    char dev_name[256] = {0};
+    int sms = 0;
+    if (cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess) {
+        std::snprintf(dev_name, sizeof(dev_name), "%s", prop.name);
+        sms = prop.multiProcessorCount;
+    }
+    char key[512];
+    std::snprintf(key, sizeof(key), "%s|sm%d|wavefront|pixels=%u|spp=%u|depth=%u|sem=%u|fast=%d|tlas=%u|blas=%u",
+                  dev_name, sms, n, tune_spp, ctx->state.depth, ctx->state.semantics, fast ? 1 : 0, ctx->tlas_len,
+                  ctx->blas_len);
+    auto entries = orn::read_tune_cache(cache_path);
+    auto hit = entries.find(key);
+    if (hit != entries.end()) {
+        const auto& f = hit->second.fields;
+        auto a = f.find("shape"), b = f.find("fetch"), c = f.find("steps");
+        // an entry outside the valid range (a hand-edited or foreign file) is
+        // tuned again
+        if (a != f.end() && b != f.end() && c != f.end() &&
+            orn::wave_config_valid((int)a->second, (int)b->second, (int)c->second)) {
+            ctx->wave_cfg = orn::WaveConfig{(int)a->second, (int)b->second, (int)c->second};
+            ctx->wave_tuned = true;
+            if (chosen) orn_wave_get_config(ctx, chosen);
+            return ORN_OK;
+        }
+    }
+    // Scratch targets and a copy of the RNG states: the context's image,
+    // progress and pixel order are untouched.
+    float4 *acc = nullptr, *fb = nullptr;
+    uint32_t* rng = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto release = [&]() {
+        if (acc) cudaFree(acc);
+        if (fb) cudaFree(fb);
+        if (rng) cudaFree(rng);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    if (cudaMalloc(&acc, (size_t)n * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&fb, (size_t)n * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&rng, (size_t)n * sizeof(uint32_t)) != cudaSuccess) {
+        release();
+        return fail(ctx, ORN_ERR_OUT_OF_MEMORY, "wavefront tuning scratch targets");
+    }
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        release();
+        return fail(ctx, ORN_ERR_CUDA, "wavefront tuning events");
+    }
+    RenderLaunch p;
+    std::memset(&p, 0, sizeof(p));
+    p.scene = ctx->scene;
+    p.pixel_count = n;
+    p.acc = acc;
+    p.fb = fb;
+    p.rng = rng;
+    p.error = ctx->d_error;
+    p.counters = ctx->d_counters;
+    p.work_counter = ctx->d_work;
+    p.shade_threshold = orn::kShadeThreshold;
+    p.cp = make_params(ctx, 1.0f);
+    p.spp = tune_spp;
+    p.do_post = 1;
+    p.order = ctx->state.pixel_order == ORN_PIXEL_ORDER_COST && ctx->order_valid ? ctx->px_order : nullptr;
+    p.cost = nullptr;
+    const int fetches[3] = {2, 4, 8};
+    const int steps[2] = {32, 64};
+    orn::WaveConfig best = ctx->wave_cfg;
+    float best_ms = 3.0e38f;
+    cudaError_t e = cudaSuccess;
+    for (int shape = 0; shape < orn::kWaveShapes && e == cudaSuccess; ++shape) {
+        for (int fi = 0; fi < 3 && e == cudaSuccess; ++fi) {
+            for (int si = 0; si < 2 && e == cudaSuccess; ++si) {
+                const orn::WaveConfig c{shape, fetches[fi], steps[si]};
+                p.wave_fetch = c.fetch;
+                p.wave_steps = c.steps;
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {   // the first run warms the caches
+                    e = cudaMemcpyAsync(rng, ctx->rng, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                                        ctx->stream);
+                    if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+                    if (e == cudaSuccess)
+                        e = orn::launch_wave(p, c, (int)ctx->state.semantics, false, fast, ctx->stream);
+                    if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                }
+                if (e == cudaSuccess && ms < best_ms) {
+                    best_ms = ms;
+                    best = c;
+                }
+                ctx->launches += 2;
+            }
+        }
+    }
+    cudaStreamSynchronize(ctx->stream);
+    release();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "wavefront tuning launch");
+    st = sync_and_check(ctx);
+    if (st) return st;
+    ctx->wave_cfg = best;
+    ctx->wave_tuned = true;
+    if (cache_path) {
+        orn::TuneEntry te;
+        te.fields["shape"] = best.shape;
+        te.fields["fetch"] = best.fetch;
+        te.fields["steps"] = best.steps;
+        te.ms = best_ms;
+        entries[key] = te;
+        orn::write_tune_cache(cache_path, entries, {"shape", "fetch", "steps"});
+    }
+    if (chosen) orn_wave_get_config(ctx, chosen);
     return ORN_OK;
 }
 

@@ -114,7 +114,31 @@ struct RenderLaunch {
     CacheLaunch cache;         // cached launches only
     const uint32_t* order;     // hand-out order of the pixels (null: raster order)
     uint32_t* cost;            // per-pixel traversal steps of this launch (or null)
+    int wave_fetch;            // wavefront kernels: idle lanes a traversing warp gathers before taking rays
+    int wave_steps;            // wavefront kernels: node visits per traversal round
 };
+
+// Launch parameters of the persistent wavefront (wave.cu): one of the
+// compiled block shapes (warps per block, of which shading, path slots per
+// block, resident blocks per SM — see wave_shape_info), the idle lanes a
+// traversing warp gathers before it takes new rays, and the node visits per
+// traversal round.  Every configuration renders the same images; only the
+// speed differs.
+struct WaveConfig {
+    int shape;
+    int fetch;
+    int steps;
+};
+constexpr int kWaveShapes = 4;
+constexpr WaveConfig kWaveDefault = {0, 4, 32};
+// The cached wavefront (wave_cached.cu) has one shape and takes these.
+constexpr int kWaveFetchDefault = 4, kWaveStepsDefault = 32;
+__host__ __device__ constexpr bool wave_config_valid(int shape, int fetch, int steps) {
+    return shape >= 0 && shape < kWaveShapes && fetch >= 1 && fetch <= 32 && steps >= 4 && steps <= 256;
+}
+// Warps, shading warps, path slots per block and resident blocks per SM of
+// compiled shape `shape` (false when there is none).
+bool wave_shape_info(int shape, int* warps, int* shading, int* slots, int* blocks_per_sm);
 
 // What orn_render_noalloc (noalloc.cu) takes from a context (capi.cu keeps
 // the context type private): its scene, device and semantics, whether the
@@ -217,7 +241,8 @@ cudaError_t launch_relmse(const float4* acc, const double* acc64, const double* 
                           double* out, cudaStream_t s);
 // The persistent wavefront (wave.cu): one launch renders p.spp passes of
 // every pixel, like launch_mega.
-cudaError_t launch_wave(const RenderLaunch& p, int semantics, bool count, bool fast, cudaStream_t s);
+cudaError_t launch_wave(const RenderLaunch& p, const WaveConfig& c, int semantics, bool count, bool fast,
+                        cudaStream_t s);
 cudaError_t launch_wf_logic(const WaveLaunch& p, uint32_t iter, int semantics, int math, bool count,
                             cudaStream_t s);
 cudaError_t launch_wf_extend(const WaveLaunch& p, uint32_t iter, bool count, bool fast, cudaStream_t s);

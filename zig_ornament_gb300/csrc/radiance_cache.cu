@@ -12,16 +12,21 @@
 // in TMEM; backward in BF16 (gradients need BF16's range) with FP32
 // accumulation; FP32 master weights, FP32 Adam.
 //
-// Every GEMM is a tcgen05.mma with M = 128 rows (one tile of 128 samples per
-// CTA, one thread per sample) and both operands K-major in shared memory
-// (tc_mma.cuh):
+// Every GEMM is a tcgen05.mma with M = 128 rows (a tile of 128 samples, one
+// thread per sample, a group of 4 warps per tile in flight) and operands in
+// shared memory (tc_mma.cuh):
 //   rc_forward      X·W1ᵀ → ReLU → ·W2ᵀ … → ·W6ᵀ, activations kept in shared
-//                   memory between layers; training also stores H1..H5 and
-//                   the relative-L2 loss gradient dZ6.
-//   rc_backward     dZ6·W6 ⊙ [H5>0] = dZ5, … down to dZ1 (BF16).
-//   rc_wgrad        dWlᵀ = Σ_tiles H(l-1)ᵀ·dZl: operands staged transposed
-//                   (features × samples), accumulated across sample tiles
-//                   in TMEM, then added to the FP32 gradient.
+//                   memory between layers, two tiles in flight per CTA;
+//                   training also stores H1..H5 and the relative-L2 loss
+//                   gradient dZ6.
+//   rc_backward     dZ6·W6 ⊙ [H5>0] = dZ5, … down to dZ1 (BF16); a layer's
+//                   H rows are fetched while its MMA runs.
+//   rc_wgrad        dWlᵀ = Σ_tiles H(l-1)ᵀ·dZl: both operands MN-major
+//                   (each sample's features are stored as they come, 16
+//                   bytes at a time), double-buffered so the next tile is
+//                   staged while the MMAs of the current one run,
+//                   accumulated across sample tiles in TMEM, then added to
+//                   the FP32 gradient.
 //   rc_adam         Adam on the FP32 master weights; rewrites the FP16
 //                   forward and BF16 backward operand copies in the K-major
 //                   layout so kernels copy them to shared memory verbatim.
@@ -89,25 +94,47 @@ __host__ __device__ constexpr uint32_t bwd_offset(int l) {
     return o;
 }
 
-// The CTA's synchronisation state for its MMA rounds.
+// The 128 threads of a tile group meet at named barrier `id` (1 + the
+// group; barrier 0 is __syncthreads'); the second form also returns whether
+// `v` holds for all of them.
+__device__ __forceinline__ void group_bar(uint32_t id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool group_bar_and(uint32_t id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.and.pred p, %2, 128, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+// A tile group's synchronisation state for its MMA rounds: its mbarrier,
+// the phase it waits for next, whether every wait so far completed, and its
+// named barrier.
 struct Sync {
     uint64_t* mbar;
     uint32_t phase;
     bool ok;
+    uint32_t bar;
 };
 
-// D(TMEM) = A · Bᵀ (+ D when `accumulate`), A: 128 x K at `a`, B: N x K at
-// `b`, both K-major.  Makes the CTA's shared-memory writes visible to the
-// tensor core, issues the K/16 MMAs from thread 0 and waits for them.  Every
-// thread must call; all threads agree on s.ok afterwards.
-__device__ __forceinline__ void gemm_round(Sync& s, uint32_t tmem, const unsigned char* a, const unsigned char* b,
-                                           uint32_t K, uint32_t N, bool bf16, bool accumulate) {
+// Issues D(TMEM) = A · Bᵀ (+ D when `accumulate`), A: 128 x K at `a`, B:
+// N x K at `b`, both K-major (or both MN-major when `mn_major`): makes the
+// group's shared-memory writes visible to the tensor core, then the group's
+// first thread issues the K/16 MMAs and commits them to the group's
+// mbarrier.  Every thread of the group calls.
+__device__ __forceinline__ void gemm_issue(Sync& s, uint32_t tmem, const unsigned char* a, const unsigned char* b,
+                                           uint32_t K, uint32_t N, bool bf16, bool accumulate,
+                                           bool mn_major = false) {
     tc::fence_async_smem();
     tc::fence_before_sync();
-    __syncthreads();
+    group_bar(s.bar);
     tc::fence_after_sync();
-    if (threadIdx.x == 0 && s.ok) {
-        const uint32_t idesc = tc::idesc_f16(128, N, bf16);
+    if ((threadIdx.x & 127u) == 0 && s.ok) {
+        const uint32_t idesc = tc::idesc_f16(128, N, bf16, mn_major);
         const uint32_t sbo = (K / 8u) * 128u;
         for (uint32_t ks = 0; ks < K / 16u; ++ks) {
             const uint64_t ad = tc::smem_desc(tc::smem_addr(a) + ks * 256u, 128u, sbo);
@@ -116,11 +143,22 @@ __device__ __forceinline__ void gemm_round(Sync& s, uint32_t tmem, const unsigne
         }
         tc::mma_commit(s.mbar);
     }
+}
+
+// Waits (bounded) for the group's issued MMAs; all its threads agree on
+// s.ok afterwards.
+__device__ __forceinline__ void gemm_wait(Sync& s) {
     const bool ok = s.ok && tc::mbar_wait(s.mbar, s.phase, 2000000000ull);
-    s.ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    s.ok = group_bar_and(s.bar, ok);
     // on failure s.phase stays the phase of the round still in flight
     if (s.ok) s.phase ^= 1u;
     tc::fence_after_sync();
+}
+
+__device__ __forceinline__ void gemm_round(Sync& s, uint32_t tmem, const unsigned char* a, const unsigned char* b,
+                                           uint32_t K, uint32_t N, bool bf16, bool accumulate) {
+    gemm_issue(s, tmem, a, b, K, N, bf16, accumulate);
+    gemm_wait(s);
 }
 
 // This thread's TMEM lane (its row of the tile), `ncols` FP32 columns.
@@ -130,61 +168,72 @@ __device__ __forceinline__ void read_row(uint32_t tmem, uint32_t ncols, float* v
     tc::tmem_ld_wait();
 }
 
-__device__ __forceinline__ uint32_t cta_setup(uint32_t* tmem_slot, uint64_t* mbar) {
+// Allocates `ncols` TMEM columns (warp 0) and initialises `nbar` mbarriers.
+__device__ __forceinline__ uint32_t cta_setup(uint32_t* tmem_slot, uint64_t* mbar, uint32_t nbar, uint32_t ncols) {
     if (threadIdx.x < 32) {
-        tc::tmem_alloc(tmem_slot, kTmemCols);
+        tc::tmem_alloc(tmem_slot, ncols);
         tc::tmem_relinquish();
     }
-    if (threadIdx.x == 0) tc::mbar_init(mbar, 1);
+    if (threadIdx.x == 0)
+        for (uint32_t i = 0; i < nbar; ++i) tc::mbar_init(mbar + i, 1);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     return *tmem_slot;
 }
 
-// After a timed-out wait: give the MMAs in flight one more bounded wait,
-// record the failure, then free the TMEM columns (on every path).  Freeing
-// while an MMA might still write them is only reached when both waits (3 s)
-// ran out; a CTA that exited holding its columns would instead leave them
+// After a timed-out wait: give the group's MMAs in flight one more bounded
+// wait, record the failure, then free the CTA's TMEM columns (on every
+// path; `tmem_base` is the allocation's first column).  Freeing while an
+// MMA might still write them is only reached when both waits (3 s) ran
+// out; a CTA that exited holding its columns would instead leave them
 // allocated for every later CTA on that SM, whose tcgen05.alloc could then
 // wait forever, so the columns are always returned.
-__device__ __forceinline__ void cta_teardown(Sync& s, uint32_t tmem, uint32_t* status) {
+__device__ __forceinline__ void cta_teardown(Sync& s, uint32_t tmem_base, uint32_t ncols, uint32_t* status) {
     if (!s.ok) {
         tc::mbar_wait(s.mbar, s.phase, 1000000000ull);
-        if (threadIdx.x == 0) atomicOr(status, 4u);   // ERR_MMA
+        if ((threadIdx.x & 127u) == 0) atomicOr(status, 4u);   // ERR_MMA
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x < 32) tc::tmem_dealloc(tmem, kTmemCols);
+    if (threadIdx.x < 32) tc::tmem_dealloc(tmem_base, ncols);
 }
 
 // ---- forward ----------------------------------------------------------------------
-// Shared memory: the six FP16 weight operands (67,584 B), X (128 x 256 FP16)
-// and two 128 x 64 activation buffers.
+// Two groups of 4 warps per CTA, each with a tile of 128 samples in flight
+// (its own X buffer, mbarrier, named barrier and 64 TMEM columns), so one
+// group's encoding and epilogues overlap the other's MMAs; group g takes
+// tiles blockIdx.x + g * gridDim.x, then every 2 * gridDim.x-th.  Shared
+// memory: the six FP16 weight operands (67,584 B) and per group X (128 x 256
+// FP16); a layer's activations overwrite the start of X (the MMA that read
+// the previous layer's has completed when they are written).
 constexpr uint32_t kWfBytes = kWeightCount * 2;
 constexpr uint32_t kXBytes = 128 * kFeatures * 2;
 constexpr uint32_t kHBytes = 128 * kHidden * 2;
-constexpr uint32_t kForwardSmem = kWfBytes + kXBytes + 2 * kHBytes;
+constexpr uint32_t kFwdGroups = 2;
+constexpr uint32_t kFwdCols = kFwdGroups * kHidden;
+constexpr uint32_t kForwardSmem = kWfBytes + kFwdGroups * kXBytes;
+static_assert(kForwardSmem <= 227u * 1024u, "forward shared memory");
 
 template <bool TRAIN>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128 * kFwdGroups, 1)
 rc_forward(RcForward p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[kFwdGroups];
     __shared__ uint32_t tmem_slot;
+    const uint32_t grp = threadIdx.x >> 7, t = threadIdx.x & 127u;
     unsigned char* W = smem;
-    unsigned char* X = smem + kWfBytes;
-    unsigned char* Hb[2] = {X + kXBytes, X + kXBytes + kHBytes};
+    unsigned char* X = smem + kWfBytes + grp * kXBytes;
     const uint32_t n = p.n_dev ? min(*p.n_dev, p.n) : p.n;
     const uint32_t tiles = (n + 127) / 128;
     if (blockIdx.x >= tiles) return;
     for (uint32_t i = threadIdx.x; i < kWfBytes / 16; i += blockDim.x)
         ((uint4*)W)[i] = __ldg((const uint4*)p.weights_f16 + i);
-    const uint32_t tmem = cta_setup(&tmem_slot, &mbar);
-    Sync s{&mbar, 0u, true};
-    const uint32_t t = threadIdx.x;
+    const uint32_t tmem_base = cta_setup(&tmem_slot, mbar, kFwdGroups, kFwdCols);
+    const uint32_t tmem = tmem_base + grp * kHidden;
+    Sync s{&mbar[grp], 0u, true, 1u + grp};
     float loss = 0.0f;
-    for (uint32_t tile = blockIdx.x; tile < tiles && s.ok; tile += gridDim.x) {
+    for (uint32_t tile = blockIdx.x + grp * gridDim.x; tile < tiles && s.ok; tile += kFwdGroups * gridDim.x) {
         const uint32_t row = tile * 128 + t;
         const bool valid = row < n;
         float in[kInputs];
@@ -204,7 +253,7 @@ rc_forward(RcForward p) {
             if (!s.ok) break;
             read_row(tmem, N, v);
             if (l < kLayers - 1) {
-                unsigned char* Hn = Hb[l & 1];
+                unsigned char* Hn = X;
                 for (uint32_t c0 = 0; c0 < kHidden; c0 += 8) {
                     uint16_t h[8];
 #pragma unroll
@@ -256,7 +305,7 @@ rc_forward(RcForward p) {
         for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
         if ((threadIdx.x & 31) == 0) atomicAdd(p.loss, loss);
     }
-    cta_teardown(s, tmem, p.status);
+    cta_teardown(s, tmem_base, kFwdCols, p.status);
 }
 
 // ---- backward (data) ----------------------------------------------------------------
@@ -276,8 +325,8 @@ rc_backward(RcBackward p) {
     if (blockIdx.x >= tiles) return;
     for (uint32_t i = threadIdx.x; i < kWbBytes / 16; i += blockDim.x)
         ((uint4*)W)[i] = __ldg((const uint4*)p.weights_bf16 + i);
-    const uint32_t tmem = cta_setup(&tmem_slot, &mbar);
-    Sync s{&mbar, 0u, true};
+    const uint32_t tmem = cta_setup(&tmem_slot, &mbar, 1, kTmemCols);
+    Sync s{&mbar, 0u, true, 1u};
     const uint32_t t = threadIdx.x;
     for (uint32_t tile = blockIdx.x; tile < tiles && s.ok; tile += gridDim.x) {
         const uint32_t row = tile * 128 + t;
@@ -295,14 +344,20 @@ rc_backward(RcBackward p) {
         float v[kHidden];
         for (int l = kLayers - 1; l >= 1; --l) {
             // dH(l-1) = dZ(l) · W(l); the B operand is W(l)ᵀ (rows = layer inputs)
-            gemm_round(s, tmem, A, W + bwd_offset(l) * 2, K, kHidden, true, false);
+            gemm_issue(s, tmem, A, W + bwd_offset(l) * 2, K, kHidden, true, false);
+            // the sample's H(l-1) row is fetched while the MMAs run
+            const uint16_t* h = p.h + ((size_t)(l - 1) * p.n + (valid ? row : 0)) * kHidden;
+            uint4 hrow[kHidden / 8];
+#pragma unroll
+            for (int c = 0; c < kHidden / 8; ++c)
+                hrow[c] = valid ? *(const uint4*)(h + 8 * c) : make_uint4(0, 0, 0, 0);
+            gemm_wait(s);
             if (!s.ok) break;
             read_row(tmem, kHidden, v);
             unsigned char* Dn = Db[(kLayers - l) & 1];
-            const uint16_t* h = p.h + ((size_t)(l - 1) * p.n + (valid ? row : 0)) * kHidden;
+#pragma unroll
             for (uint32_t c0 = 0; c0 < kHidden; c0 += 8) {
-                uint4 hv = valid ? *(const uint4*)(h + c0) : make_uint4(0, 0, 0, 0);
-                const uint16_t* hh = (const uint16_t*)&hv;
+                const uint16_t* hh = (const uint16_t*)&hrow[c0 / 8];
                 uint16_t d[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) d[j] = f2b(h2f(hh[j]) > 0.0f ? v[c0 + j] : 0.0f);
@@ -314,26 +369,28 @@ rc_backward(RcBackward p) {
             K = kHidden;
         }
     }
-    cta_teardown(s, tmem, p.status);
+    cta_teardown(s, tmem, kTmemCols, p.status);
 }
 
 // ---- weight gradients -------------------------------------------------------------
 // One job = (layer l, a block of up to 128 of its inputs).  For every tile of
 // 128 samples the CTA stages A = H(l-1)ᵀ (inputs x samples) and B = dZ(l)ᵀ
-// (outputs x samples), both K-major with K = samples, and accumulates
-// D[in x out] in TMEM across its tiles; D is then added to the FP32 gradient
-// (gradient of W(l)[out][in] = D[in][out]).
+// (outputs x samples), both MN-major with K = samples — thread t stores
+// sample t's inputs and output gradients 8 at a time as 16-byte chunks,
+// which keeps the stores free of bank conflicts (a K-major copy would be
+// a transpose, 2 bytes per store) — and accumulates D[in x out] in TMEM
+// across its tiles; D is then added to the FP32 gradient (gradient of
+// W(l)[out][in] = D[in][out]).  The operands are double-buffered: tile i+1
+// is staged while the MMAs of tile i run.
 constexpr uint32_t kWgA = 128 * 128 * 2;
 constexpr uint32_t kWgB = 64 * 128 * 2;
-constexpr uint32_t kWgradSmem = kWgA + kWgB;
+constexpr uint32_t kWgradSmem = 2 * (kWgA + kWgB);
 
 __global__ void __launch_bounds__(128, 1)
 rc_wgrad(RcWgrad p) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
-    unsigned char* A = smem;
-    unsigned char* B = smem + kWgA;
     const uint32_t job = blockIdx.x % kWgradJobs, split = blockIdx.x / kWgradJobs;
     const int l = job < 2 ? 0 : (int)job - 1;
     const uint32_t in_base = job < 2 ? job * 128u : 0u;
@@ -341,43 +398,61 @@ rc_wgrad(RcWgrad p) {
     const uint32_t out_n = rc_layer_out(l);
     const uint32_t tiles = (p.n + 127) / 128;
     if (split >= tiles) return;
-    const uint32_t tmem = cta_setup(&tmem_slot, &mbar);
-    Sync s{&mbar, 0u, true};
     const uint32_t t = threadIdx.x;
-    bool first = true;
-    for (uint32_t tile = split; tile < tiles && s.ok; tile += p.splits) {
+    // rows in_n..127 of A (inputs a layer does not have) stay zero
+    for (uint32_t buf = 0; buf < 2; ++buf)
+        for (uint32_t c0 = in_n; c0 < 128; c0 += 8)
+            *(uint4*)(smem + buf * kWgA + tc::mnmajor_offset(c0, t, 128)) = make_uint4(0, 0, 0, 0);
+    // Stages tile `tile` into operand buffer `buf`.
+    auto stage = [&](uint32_t tile, uint32_t buf) {
+        unsigned char* A = smem + buf * kWgA;
+        unsigned char* B = smem + 2 * kWgA + buf * kWgB;
         const uint32_t row = tile * 128 + t;
         const bool valid = row < p.n;
         if (l == 0) {
             float in[kInputs];
             for (int j = 0; j < kInputs; ++j) in[j] = valid ? p.inputs[(size_t)row * kInputs + j] : 0.0f;
+            // (features come in chunks of 8 at multiples of 8, and a block
+            // starts at a multiple of 128, so a chunk is in or out whole)
             encode(in, [&](int f0, const float* g) {
                 if ((uint32_t)f0 >= in_base && (uint32_t)f0 < in_base + 128u) {
+                    uint16_t b[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
-                        *(uint16_t*)(A + tc::kmajor_offset((uint32_t)f0 - in_base + j, t, 128)) =
-                            valid ? f2b(g[j]) : (uint16_t)0;
+                    for (int j = 0; j < 8; ++j) b[j] = valid ? f2b(g[j]) : (uint16_t)0;
+                    *(uint4*)(A + tc::mnmajor_offset((uint32_t)f0 - in_base, t, 128)) = pack8(b);
                 }
             });
         } else {
             const uint16_t* h = p.h + ((size_t)(l - 1) * p.n + (valid ? row : 0)) * kHidden;
-            for (uint32_t c0 = 0; c0 < 128; c0 += 8) {
-                uint4 hv = (valid && c0 < in_n) ? *(const uint4*)(h + c0) : make_uint4(0, 0, 0, 0);
-                const uint16_t* hh = (const uint16_t*)&hv;
 #pragma unroll
-                for (int j = 0; j < 8; ++j) *(uint16_t*)(A + tc::kmajor_offset(c0 + j, t, 128)) = f2b(h2f(hh[j]));
+            for (uint32_t c0 = 0; c0 < (uint32_t)kHidden; c0 += 8) {
+                const uint4 hv = valid ? *(const uint4*)(h + c0) : make_uint4(0, 0, 0, 0);
+                const uint16_t* hh = (const uint16_t*)&hv;
+                uint16_t b[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) b[j] = f2b(h2f(hh[j]));
+                *(uint4*)(A + tc::mnmajor_offset(c0, t, 128)) = pack8(b);
             }
         }
         const uint16_t* dz = l == kLayers - 1 ? p.dz6 + (size_t)(valid ? row : 0) * kOutPad
                                               : p.dz + ((size_t)l * p.n + (valid ? row : 0)) * kHidden;
         for (uint32_t c0 = 0; c0 < out_n; c0 += 8) {
-            uint4 dv = valid ? *(const uint4*)(dz + c0) : make_uint4(0, 0, 0, 0);
-            const uint16_t* dd = (const uint16_t*)&dv;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) *(uint16_t*)(B + tc::kmajor_offset(c0 + j, t, 128)) = dd[j];
+            const uint4 dv = valid ? *(const uint4*)(dz + c0) : make_uint4(0, 0, 0, 0);
+            *(uint4*)(B + tc::mnmajor_offset(c0, t, 128)) = dv;
         }
-        gemm_round(s, tmem, A, B, 128, out_n, true, !first);
+    };
+    const uint32_t tmem = cta_setup(&tmem_slot, &mbar, 1, kTmemCols);
+    Sync s{&mbar, 0u, true, 1u};
+    stage(split, 0);
+    uint32_t buf = 0;
+    bool first = true;
+    for (uint32_t tile = split; tile < tiles && s.ok; tile += p.splits) {
+        gemm_issue(s, tmem, smem + buf * kWgA, smem + 2 * kWgA + buf * kWgB, 128, out_n, true, !first, true);
+        // the other buffer's MMAs completed in the previous round
+        if (tile + p.splits < tiles) stage(tile + p.splits, buf ^ 1u);
+        gemm_wait(s);
         first = false;
+        buf ^= 1u;
     }
     if (s.ok && !first) {
         float v[kHidden];
@@ -387,7 +462,7 @@ rc_wgrad(RcWgrad p) {
             for (uint32_t o = 0; o < out_n; ++o) atomicAdd(&g[(size_t)o * rc_layer_in(l) + in_base + t], v[o]);
         }
     }
-    cta_teardown(s, tmem, p.status);
+    cta_teardown(s, tmem, kTmemCols, p.status);
 }
 
 // ---- Adam and the operand copies ------------------------------------------------------
@@ -435,8 +510,8 @@ cudaError_t rc_launch_forward(const RcForward& p, bool train, int grid, cudaStre
     cudaError_t e = train ? allow_smem(rc::rc_forward<true>, rc::kForwardSmem)
                           : allow_smem(rc::rc_forward<false>, rc::kForwardSmem);
     if (e != cudaSuccess) return e;
-    if (train) rc::rc_forward<true><<<grid, 128, rc::kForwardSmem, s>>>(p);
-    else rc::rc_forward<false><<<grid, 128, rc::kForwardSmem, s>>>(p);
+    if (train) rc::rc_forward<true><<<grid, 128 * rc::kFwdGroups, rc::kForwardSmem, s>>>(p);
+    else rc::rc_forward<false><<<grid, 128 * rc::kFwdGroups, rc::kForwardSmem, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -6,12 +6,14 @@
 //   MMA       tcgen05.mma.cta_group::1.kind::f16: D(TMEM, FP32) (+)= A(SMEM) ·
 //             B(SMEM), issued by one thread; tcgen05.commit arrives on an
 //             mbarrier when the issued MMAs have completed.
-//   Operands  K-major, no swizzle: the matrix is tiled into "core matrices"
-//             of 8 rows x 16 bytes (8 halves); a core matrix is 128
-//             contiguous bytes, row r at +16r.  Core matrix (ri, ki) sits at
-//             ri * SBO + ki * LBO from the operand base.  Here every operand
-//             uses LBO = 128 (cores adjacent along K are contiguous) and
-//             SBO = (K / 8) * 128.
+//   Operands  no swizzle, tiled into "core matrices" of 8 x 8 elements
+//             (16-bit), each 128 contiguous bytes in 8 rows of 16 bytes.
+//             K-major: a core row holds 8 consecutive K of one M/N row.
+//             MN-major: a core row holds 8 consecutive M/N of one K.
+//             Either way the core matrix covering (M/N block mi, K block ki)
+//             sits at mi * SBO + ki * LBO from the operand base; here every
+//             operand uses LBO = 128 (cores adjacent along K are contiguous)
+//             and SBO = (K / 8) * 128.
 //   Waits     every mbarrier wait is bounded by %globaltimer; on timeout the
 //             caller records an error and skips the rest of its work.
 #pragma once
@@ -106,10 +108,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 }
 
 // Instruction descriptor for kind::f16: FP32 accumulator (bits 4-5 = 1),
-// A and B both F16 (0) or both BF16 (1) (bits 7-9, 10-12), both K-major
-// (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-__host__ __device__ constexpr uint32_t idesc_f16(uint32_t m, uint32_t n, bool bf16) {
-    return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+// A and B both F16 (0) or both BF16 (1) (bits 7-9, 10-12), A and B K-major
+// (bits 15, 16 = 0) or MN-major (1), N >> 3 at bits 17-22, M >> 4 at bits
+// 24-28.
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t m, uint32_t n, bool bf16, bool mn_major = false) {
+    return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((mn_major ? 1u : 0u) << 15) |
+           ((mn_major ? 1u : 0u) << 16) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
 
 // D[tmem] (+)= A · B, one thread issues.
@@ -135,6 +139,14 @@ __device__ __forceinline__ void mma_commit(uint64_t* mbar) {
 // columns (LBO = 128, SBO = K/8 * 128).
 __host__ __device__ __forceinline__ uint32_t kmajor_offset(uint32_t r, uint32_t k, uint32_t K) {
     return (r >> 3) * (K >> 3) * 128u + (k >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// Byte offset of element (r, k) of an MN-major no-swizzle operand with K
+// columns (same LBO and SBO): 8 consecutive r of one k are 16 contiguous
+// bytes, so a row of the source matrix stored k by k lands as whole
+// 16-byte chunks.
+__host__ __device__ __forceinline__ uint32_t mnmajor_offset(uint32_t r, uint32_t k, uint32_t K) {
+    return (r >> 3) * (K >> 3) * 128u + (k >> 3) * 128u + (k & 7u) * 16u + (r & 7u) * 2u;
 }
 
 }  // namespace tc

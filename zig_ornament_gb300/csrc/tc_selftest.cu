@@ -2,11 +2,12 @@
 // instruction descriptor encodings (tc_mma.cuh) against a host GEMM.
 //
 // D[128 x N] = A[128 x K] · B[N x K]^T with A and B given row-major (K
-// contiguous) in global memory, staged into the K-major no-swizzle layout,
-// multiplied with K/16 tcgen05.mma instructions into TMEM and read back with
-// tcgen05.ld.  `swap_offsets` exchanges the two byte offsets in the operand
-// descriptors (for the self-test to tell the encodings apart); both forms
-// address only the 64 KiB operand regions below.
+// contiguous) in global memory, staged into the K-major no-swizzle layout
+// (or the MN-major one, mode bit 1), multiplied with K/16 tcgen05.mma
+// instructions into TMEM and read back with tcgen05.ld.  Mode bit 0
+// exchanges the two byte offsets in the operand descriptors (for the
+// self-test to tell the encodings apart); every form addresses only the
+// 64 KiB operand regions below.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -21,17 +22,26 @@ constexpr uint32_t kSelfTestRegion = 64 * 1024;
 
 __global__ void __launch_bounds__(128)
 tc_selftest_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ B, float* __restrict__ D,
-                   uint32_t K, uint32_t N, uint32_t bf16, uint32_t swap_offsets, uint32_t* status) {
+                   uint32_t K, uint32_t N, uint32_t bf16, uint32_t mode, uint32_t* status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     unsigned char* sa = smem;
     unsigned char* sb = smem + kSelfTestRegion;
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    // stage A (128 rows) and B (N rows), 16-byte chunks
-    for (uint32_t k = 0; k < K; k += 8) {
-        *(uint4*)(sa + tc::kmajor_offset(tid, k, K)) = *(const uint4*)(A + (size_t)tid * K + k);
-        if (tid < N) *(uint4*)(sb + tc::kmajor_offset(tid, k, K)) = *(const uint4*)(B + (size_t)tid * K + k);
+    const bool swap_offsets = (mode & 1u) != 0, mn_major = (mode & 2u) != 0;
+    // stage A (128 rows) and B (N rows): 16-byte chunks (K-major) or single
+    // elements (MN-major)
+    if (mn_major) {
+        for (uint32_t k = 0; k < K; ++k) {
+            *(uint16_t*)(sa + tc::mnmajor_offset(tid, k, K)) = A[(size_t)tid * K + k];
+            if (tid < N) *(uint16_t*)(sb + tc::mnmajor_offset(tid, k, K)) = B[(size_t)tid * K + k];
+        }
+    } else {
+        for (uint32_t k = 0; k < K; k += 8) {
+            *(uint4*)(sa + tc::kmajor_offset(tid, k, K)) = *(const uint4*)(A + (size_t)tid * K + k);
+            if (tid < N) *(uint4*)(sb + tc::kmajor_offset(tid, k, K)) = *(const uint4*)(B + (size_t)tid * K + k);
+        }
     }
     if (warp == 0) {
         tc::tmem_alloc(&tmem_base, 128);
@@ -45,7 +55,7 @@ tc_selftest_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ 
     const uint32_t tmem = tmem_base;
     const uint32_t lbo = 128u, sbo = (K / 8u) * 128u;
     if (tid == 0) {
-        const uint32_t idesc = tc::idesc_f16(128, N, bf16 != 0);
+        const uint32_t idesc = tc::idesc_f16(128, N, bf16 != 0, mn_major);
         for (uint32_t ks = 0; ks < K / 16u; ++ks) {
             uint32_t off = ks * 2u * 128u;
             uint64_t ad = swap_offsets ? tc::smem_desc(tc::smem_addr(sa) + off, sbo, lbo)
@@ -78,9 +88,9 @@ tc_selftest_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ 
 
 }  // namespace orn
 
-extern "C" int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int swap_offsets, const uint16_t* A,
+extern "C" int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int mode, const uint16_t* A,
                                const uint16_t* B, float* D) {
-    if (!A || !B || !D || K == 0 || K > 256 || K % 16 || N < 16 || N > 128 || N % 16)
+    if (!A || !B || !D || K == 0 || K > 256 || K % 16 || N < 16 || N > 128 || N % 16 || mode < 0 || mode > 3)
         return ORN_ERR_INVALID_ARGUMENT;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return ORN_ERR_NO_DEVICE;
@@ -99,7 +109,7 @@ extern "C" int orn_tc_selftest(uint32_t K, uint32_t N, int bf16, int swap_offset
                                     (int)smem) != cudaSuccess) {
         st = ORN_ERR_CUDA;
     } else {
-        orn::tc_selftest_kernel<<<1, 128, smem>>>(dA, dB, dD, K, N, bf16 ? 1u : 0u, swap_offsets ? 1u : 0u, dS);
+        orn::tc_selftest_kernel<<<1, 128, smem>>>(dA, dB, dD, K, N, bf16 ? 1u : 0u, (uint32_t)mode, dS);
         uint32_t s = 0;
         if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
             cudaMemcpy(&s, dS, 4, cudaMemcpyDeviceToHost) != cudaSuccess ||

@@ -10,9 +10,10 @@
 //   ray queue  slots whose next ray is ready to trace;
 //   hit queue  slots whose ray was traced (or that need a pixel).
 //
-// The block's warps (wave_queue.cuh, wave_warp) split the work: seven of the
-// eight traverse — idle lanes take the next rays from the ray queue
-// (ballot-compacted, one reservation per warp) once four of them are idle,
+// The block's warps (wave_queue.cuh) split the work: all but one traverse
+// (traversal_warp; nine of ten in the default block shape) — idle lanes
+// take the next rays from the ray queue (ballot-compacted, one reservation
+// per warp) once enough of them are idle (p.wave_fetch, default four),
 // each lane visits BVH nodes (walker_step, the megakernel's traversal) and,
 // when its ray is done, writes the hit record into the slot and appends the
 // slot to the hit queue — and one shades: it takes up to 32 slots from the
@@ -61,12 +62,10 @@ struct Pool {
 
 }  // namespace
 
-#ifndef ORN_WAVE_MIN_BLOCKS
-#define ORN_WAVE_MIN_BLOCKS 3
-#endif
-
-template <int SEM, bool COUNT, bool FAST, int NW, int NS, int P>
-__global__ void __launch_bounds__(32 * NW, ORN_WAVE_MIN_BLOCKS)
+// NW warps per block, NS of them shading, P path slots, launch bounds for
+// MINB resident blocks per SM (the register cap).
+template <int SEM, bool COUNT, bool FAST, int NW, int NS, int P, int MINB>
+__global__ void __launch_bounds__(32 * NW, MINB)
 wave_kernel(RenderLaunch p) {
     extern __shared__ __align__(16) unsigned char wave_smem[];
     Pool<P>& pool = *reinterpret_cast<Pool<P>*>(wave_smem);
@@ -268,27 +267,46 @@ wave_kernel(RenderLaunch p) {
 // ---- host-side launcher ------------------------------------------------------------
 namespace {
 
-// warps per block and path slots per block (the slots outnumber the lanes,
-// so lanes find rays while other paths wait to be shaded)
-#ifndef ORN_WAVE_WARPS
-#define ORN_WAVE_WARPS 8
-#endif
-#ifndef ORN_WAVE_SLOTS
-#define ORN_WAVE_SLOTS 256
-#endif
-// warps of a block that shade (the others traverse)
-#ifndef ORN_WAVE_SHADERS
-#define ORN_WAVE_SHADERS 1
-#endif
-constexpr int kWaveW = ORN_WAVE_WARPS, kWaveP = ORN_WAVE_SLOTS, kWaveS = ORN_WAVE_SHADERS;
+// The compiled block shapes (WaveConfig::shape, orn_wave_config.shape):
+// warps per block, shading warps among them, path slots per block (more
+// slots than traversal lanes, so lanes find rays while other paths wait to
+// be shaded) and the resident blocks per SM the registers are capped for.
+// Measured on the 1080p plain workload (Msamples/s; the megakernel 365):
+// 10 warps (9 + 1) x 2 blocks 354, 11 + 1 x 2 blocks 329, 7 + 1 x 3 blocks
+// 320 (80 registers); also tried: 8 + 2 x 2 blocks 325, 6 + 2 x 3 blocks
+// 284, 5 + 1 x 4 blocks 308, 7 + 1 x 2 blocks 304, 14 + 2 x 1 block 305.
+template <int SHAPE>
+struct Shape;
+template <>
+struct Shape<0> {
+    static constexpr int W = 10, S = 1, P = 320, B = 2;
+};
+template <>
+struct Shape<1> {
+    static constexpr int W = 8, S = 1, P = 256, B = 3;
+};
+template <>
+struct Shape<2> {
+    static constexpr int W = 12, S = 1, P = 384, B = 2;
+};
+template <>
+struct Shape<3> {
+    static constexpr int W = 11, S = 1, P = 352, B = 2;
+};
 
-template <int SEM, bool COUNT, bool FAST>
+template <int SHAPE>
+constexpr size_t shape_smem() {
+    using T = Shape<SHAPE>;
+    return ((sizeof(Pool<T::P>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * 32 * (T::W - T::S);
+}
+
+template <int SEM, bool COUNT, bool FAST, int SHAPE>
 cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
-    constexpr int kBlock = 32 * kWaveW;
-    constexpr size_t kSmem =
-        ((sizeof(Pool<kWaveP>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * 32 * (kWaveW - kWaveS);
+    using T = Shape<SHAPE>;
+    constexpr int kBlock = 32 * T::W;
+    constexpr size_t kSmem = shape_smem<SHAPE>();
     static int blocks_per_sm = 0, sms = 0;
-    auto kern = wave_kernel<SEM, COUNT, FAST, kWaveW, kWaveS, kWaveP>;
+    auto kern = wave_kernel<SEM, COUNT, FAST, T::W, T::S, T::P, T::B>;
     // more than 48 KB of dynamic shared memory: an opt-in per device
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
     if (e != cudaSuccess) return e;
@@ -300,7 +318,7 @@ cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     // enough blocks for every pixel to have a slot, at most one wave of resident blocks
-    uint32_t need = (p.pixel_count + kWaveP - 1) / kWaveP;
+    uint32_t need = (p.pixel_count + T::P - 1) / T::P;
     uint32_t grid = (uint32_t)(blocks_per_sm * sms);
     if (need < grid) grid = need;
     e = cudaMemsetAsync(p.work_counter, 0, sizeof(uint32_t), s);
@@ -309,15 +327,45 @@ cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// Counting launches (a diagnostics mode) are compiled for shape 0 only.
+template <int SEM, bool FAST>
+cudaError_t launch_wave_shape(const RenderLaunch& p, int shape, bool count, cudaStream_t s) {
+    if (count) return launch_wave_t<SEM, true, FAST, 0>(p, s);
+    switch (shape) {
+        case 1: return launch_wave_t<SEM, false, FAST, 1>(p, s);
+        case 2: return launch_wave_t<SEM, false, FAST, 2>(p, s);
+        case 3: return launch_wave_t<SEM, false, FAST, 3>(p, s);
+        default: return launch_wave_t<SEM, false, FAST, 0>(p, s);
+    }
+}
+
 }  // namespace
 
-cudaError_t launch_wave(const RenderLaunch& p, int semantics, bool count, bool fast, cudaStream_t s) {
-    if (semantics == SEM_WGSL) {
-        if (fast) return count ? launch_wave_t<SEM_WGSL, true, true>(p, s) : launch_wave_t<SEM_WGSL, false, true>(p, s);
-        return count ? launch_wave_t<SEM_WGSL, true, false>(p, s) : launch_wave_t<SEM_WGSL, false, false>(p, s);
+bool wave_shape_info(int shape, int* warps, int* shading, int* slots, int* blocks_per_sm) {
+    int w = 0, sh = 0, sl = 0, b = 0;
+    switch (shape) {
+        case 0: w = Shape<0>::W; sh = Shape<0>::S; sl = Shape<0>::P; b = Shape<0>::B; break;
+        case 1: w = Shape<1>::W; sh = Shape<1>::S; sl = Shape<1>::P; b = Shape<1>::B; break;
+        case 2: w = Shape<2>::W; sh = Shape<2>::S; sl = Shape<2>::P; b = Shape<2>::B; break;
+        case 3: w = Shape<3>::W; sh = Shape<3>::S; sl = Shape<3>::P; b = Shape<3>::B; break;
+        default: return false;
     }
-    if (fast) return count ? launch_wave_t<SEM_HIP, true, true>(p, s) : launch_wave_t<SEM_HIP, false, true>(p, s);
-    return count ? launch_wave_t<SEM_HIP, true, false>(p, s) : launch_wave_t<SEM_HIP, false, false>(p, s);
+    if (warps) *warps = w;
+    if (shading) *shading = sh;
+    if (slots) *slots = sl;
+    if (blocks_per_sm) *blocks_per_sm = b;
+    return true;
+}
+
+cudaError_t launch_wave(const RenderLaunch& p, const WaveConfig& c, int semantics, bool count, bool fast,
+                        cudaStream_t s) {
+    if (!wave_config_valid(c.shape, c.fetch, c.steps) || p.wave_fetch != c.fetch || p.wave_steps != c.steps)
+        return cudaErrorInvalidValue;
+    if (semantics == SEM_WGSL)
+        return fast ? launch_wave_shape<SEM_WGSL, true>(p, c.shape, count, s)
+                    : launch_wave_shape<SEM_WGSL, false>(p, c.shape, count, s);
+    return fast ? launch_wave_shape<SEM_HIP, true>(p, c.shape, count, s)
+                : launch_wave_shape<SEM_HIP, false>(p, c.shape, count, s);
 }
 
 }  // namespace orn

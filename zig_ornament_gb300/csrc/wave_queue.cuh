@@ -19,16 +19,6 @@ namespace orn {
 namespace wave {
 
 constexpr uint32_t kEmpty = 0xffffffffu;
-// idle lanes of a traversing warp needed before it takes new rays
-#ifndef ORN_WAVE_FETCH
-#define ORN_WAVE_FETCH 4
-#endif
-constexpr int kWaveFetch = ORN_WAVE_FETCH;
-// node visits per traversal round (between refills from the ray queue)
-#ifndef ORN_WAVE_STEPS
-#define ORN_WAVE_STEPS 32
-#endif
-constexpr int kWaveSteps = ORN_WAVE_STEPS;
 constexpr uint64_t kWaitLimitNs = 5000000000ull;   // 5 s: any real wait is microseconds
 enum SlotFlag { HIT_MISS = 0, HIT_ANY = 1, HIT_FAILED = 2, NEED_PIXEL = 3 };
 // What a warp of a wavefront block does (wave_warp): both kinds of work, only
@@ -126,10 +116,10 @@ __device__ __forceinline__ uint32_t q_pop(uint32_t* q, uint32_t* head, const uin
 // The loop every warp of a wavefront block runs.  A warp switches between
 // the two kinds of work by the state of its own lanes and of the queues:
 //   * while any lane has a ray in flight it traverses: every such lane
-//     visits up to kWaveSteps BVH nodes per round (walker_step), a finished
-//     ray's hit record goes into its slot and the slot into the hit queue,
-//     and idle lanes take the next rays from the ray queue once kWaveFetch
-//     of them are idle;
+//     visits up to p.wave_steps BVH nodes per round (walker_step), a
+//     finished ray's hit record goes into its slot and the slot into the hit
+//     queue, and idle lanes take the next rays from the ray queue once
+//     p.wave_fetch of them are idle;
 //   * once none has, it shades — 32 queued hits at a time, or whatever is
 //     queued when no ray is waiting — through `shade(slot)` (called by all
 //     32 lanes with the lane's slot or kEmpty; it runs the path logic, queues
@@ -158,6 +148,7 @@ __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uin
     stack.sstack = sstack;
     stack.sstride = stride;
     const float t_min = p.cp.ray_cast_epsilon;
+    const int fetch = p.wave_fetch, round_steps = p.wave_steps;
     uint32_t slot = kEmpty, steps = 0;
     f3 ro = mk(0.0f, 0.0f, 0.0f), rd = ro;
     HitRec h;
@@ -192,7 +183,7 @@ __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uin
             }
         }
         const unsigned idle = __ballot_sync(kFull, slot == kEmpty);
-        if (idle != 0u && ((int)__popc(idle) >= kWaveFetch || idle == kFull)) {
+        if (idle != 0u && ((int)__popc(idle) >= fetch || idle == kFull)) {
             const uint32_t got = q_pop<P>(pool.rq, &pool.rq_head, &pool.rq_tail, idle, lane, &ok);
             if (got != kEmpty) {
                 slot = got;
@@ -215,7 +206,7 @@ __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uin
         uint32_t flag = HIT_MISS;
         if (slot != kEmpty) {
 #pragma unroll 1
-            for (int s = 0; s < kWaveSteps; ++s) {
+            for (int s = 0; s < round_steps; ++s) {
                 ++steps;
                 const uint32_t e0 = err;
                 if (!walker_step<COUNT, kSmemStack, FAST, ANY>(w, p.scene, ro, rd, t_min, &h, stack, &vc, &err)) {
@@ -242,9 +233,9 @@ __device__ __forceinline__ void wave_warp(Pool& pool, const RenderLaunch& p, uin
     }
 }
 
-// A warp that only traverses (the plain wavefront's seven of eight): idle
-// lanes take rays from the ray queue once kWaveFetch of them are idle (or
-// all are), every lane with a ray visits up to kWaveSteps BVH nodes per
+// A warp that only traverses (the plain wavefront's traversal warps): idle
+// lanes take rays from the ray queue once p.wave_fetch of them are idle (or
+// all are), every lane with a ray visits up to p.wave_steps BVH nodes per
 // round, and a finished ray's hit record goes into its slot, the slot into
 // the hit queue.  The same traversal as wave_warp's, in a loop that carries
 // no shading code (measured: 331 against 274 Msamples/s for wave_warp with
@@ -258,6 +249,8 @@ __device__ __forceinline__ void traversal_warp(Pool& pool, const RenderLaunch& p
     stack.sstack = sstack;
     stack.sstride = stride;
     const float t_min = p.cp.ray_cast_epsilon;
+    const int fetch = p.wave_fetch;
+    const uint32_t round_steps = (uint32_t)p.wave_steps;
     uint32_t slot = kEmpty, steps = 0;
     f3 ro = mk(0.0f, 0.0f, 0.0f), rd = ro;
     HitRec h;
@@ -267,7 +260,7 @@ __device__ __forceinline__ void traversal_warp(Pool& pool, const RenderLaunch& p
     for (;;) {
         if (warp_flag(vload(pool.abort) != 0u)) break;
         const unsigned idle = __ballot_sync(kFull, slot == kEmpty);
-        if (idle != 0u && ((int)__popc(idle) >= kWaveFetch || idle == kFull)) {
+        if (idle != 0u && ((int)__popc(idle) >= fetch || idle == kFull)) {
             const uint32_t got = q_pop<P>(pool.rq, &pool.rq_head, &pool.rq_tail, idle, lane, &ok);
             if (got != kEmpty) {
                 slot = got;
@@ -304,7 +297,7 @@ __device__ __forceinline__ void traversal_warp(Pool& pool, const RenderLaunch& p
             uint32_t s = 0;
             const uint32_t e0 = err;
 #pragma unroll 1
-            while (s < (uint32_t)kWaveSteps) {
+            while (s < round_steps) {
                 ++s;
                 if (!walker_step<COUNT, kSmemStack, FAST, false, COUNT>(w, p.scene, ro, rd, t_min, &h, stack, &vc,
                                                                         &err)) {

@@ -785,6 +785,27 @@ class Renderer:
         self._check(self._lib.orn_attach_cache(self._ctx, cache.handle if cache is not None else None))
         self._cache = cache   # keep it alive while attached
 
+    @staticmethod
+    def _wave_dict(c) -> dict:
+        return {"shape": c.shape, "fetch": c.fetch, "steps": c.steps, "tuned": bool(c.tuned)}
+
+    def wave_config(self) -> dict:
+        """Launch parameters of KERNEL_WAVEFRONT renders (orn_wave_get_config)."""
+        c = _lib.WaveConfig()
+        self._check(self._lib.orn_wave_get_config(self._ctx, C.byref(c)))
+        return self._wave_dict(c)
+
+    def set_wave_config(self, shape: int = 0, fetch: int = 4, steps: int = 32):
+        self._check(self._lib.orn_wave_set_config(self._ctx, C.byref(_lib.WaveConfig(shape, fetch, steps, 0))))
+
+    def wave_tune(self, cache_path: Optional[str] = None) -> dict:
+        """Autotune the wavefront's launch parameters for the current scene,
+        camera, resolution and state (orn_wave_tune); returns the choice."""
+        c = _lib.WaveConfig()
+        path = str(cache_path).encode() if cache_path else None
+        self._check(self._lib.orn_wave_tune(self._ctx, path, C.byref(c)))
+        return self._wave_dict(c)
+
 
 class RadianceCache:
     """The learned radiance cache (orn_cache_*): a 10-input, 5 x 64 ReLU,
