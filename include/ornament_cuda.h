@@ -286,17 +286,17 @@ typedef struct orn_wave_config {
                          3 = 11 warps (10 + 1), 352 slots, 2 blocks per SM */
     uint32_t fetch;   /* idle lanes a traversing warp gathers before it takes
                          new rays: 1..32 (default 4) */
-    uint32_t steps;   /* node visits per traversal round: 4..256 (default 32) */
+    uint32_t steps;   /* node visits per traversal round: 32 (default) or 64 */
     uint32_t tuned;   /* out: 1 when chosen by orn_wave_tune */
 } orn_wave_config;
 int orn_wave_get_config(const orn_context* ctx, orn_wave_config* out);
 /* ORN_ERR_INVALID_ARGUMENT outside the ranges above. */
 int orn_wave_set_config(orn_context* ctx, orn_wave_config const* config);
 /* Autotuner: renders one launch (the passes orn_render would put in one
- * launch, at most 8) of the context's current scene, camera, resolution and
- * state with every candidate (4 shapes x fetch 2/4/8 x steps 32/64) into
- * scratch targets — the context's image, RNG states and pixel order are not
- * touched — and keeps the fastest.  With `cache_path`, a JSON file keyed by
+ * launch, at most 8 and at most ~16 M samples) of the context's current
+ * scene, camera, resolution and state with every candidate (4 shapes x
+ * fetch 2/4/8 x steps 32/64) into scratch targets — the context's image,
+ * RNG states and pixel order are not touched — and keeps the fastest.  With `cache_path`, a JSON file keyed by
  * device and workload (pixels, passes, depth, semantics, tree sizes) is
  * read first and updated after tuning.  `chosen` may be NULL.
  * Synchronous. */

@@ -542,7 +542,6 @@ int render_cached(orn_context* ctx, RenderLaunch p, uint32_t passes, float ci_st
     p.spp = 1;
     p.shade_threshold = orn::kCacheShadeThreshold;
     p.wave_fetch = orn::kWaveFetchDefault;
-    p.wave_steps = orn::kWaveStepsDefault;
     const uint32_t streams = ctx->cq_streams;
     p.cache.streams = streams;
     p.cache.rng_extra = ctx->rng_extra;
@@ -993,7 +992,6 @@ int orn_render(orn_context* ctx) {
     p.work_counter = ctx->d_work;
     p.shade_threshold = orn::kShadeThreshold;
     p.wave_fetch = ctx->wave_cfg.fetch;
-    p.wave_steps = ctx->wave_cfg.steps;
     if (ctx->counters_enabled)
         ORN_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, ORN_COUNTER_COUNT * sizeof(unsigned long long), ctx->stream));
     if (is_cached(ctx)) {
@@ -1256,10 +1254,10 @@ int orn_wave_get_config(const orn_context* ctx, orn_wave_config* out) {
 
 int orn_wave_set_config(orn_context* ctx, const orn_wave_config* c) {
     if (!ctx || !c) return ORN_ERR_INVALID_ARGUMENT;
-    if (c->shape >= (uint32_t)orn::kWaveShapes || c->fetch > 32u || c->steps > 256u ||
+    if (c->shape >= (uint32_t)orn::kWaveShapes || c->fetch > 32u || c->steps > 64u ||
         !orn::wave_config_valid((int)c->shape, (int)c->fetch, (int)c->steps))
         return fail(ctx, ORN_ERR_INVALID_ARGUMENT,
-                    "invalid wavefront configuration (shape 0..3, fetch 1..32, steps 4..256)");
+                    "invalid wavefront configuration (shape 0..3, fetch 1..32, steps 32 or 64)");
     ctx->wave_cfg = orn::WaveConfig{(int)c->shape, (int)c->fetch, (int)c->steps};
     ctx->wave_tuned = false;
     return ORN_OK;
@@ -1275,10 +1273,12 @@ int orn_wave_tune(orn_context* ctx, const char* cache_path, orn_wave_config* cho
     if (st) return st;
     const uint32_t n = ctx->width * ctx->height;
     // the passes of one launch as orn_render would issue them, at most 8
+    // and at most ~16 M samples per candidate launch
     const uint32_t passes = std::max<uint32_t>(ctx->state.iterations, 1u);
     uint32_t chunk = ctx->state.spp_per_launch;
     if (chunk == 0) chunk = passes <= 64 ? passes : 32;
-    const uint32_t tune_spp = std::min<uint32_t>(chunk, 8u);
+    const uint32_t tune_spp =
+        std::max<uint32_t>(1u, std::min<uint32_t>({chunk, 8u, (uint32_t)((16u << 20) / std::max<uint32_t>(n, 1u))}));
     const bool fast = render_fast_slabs(ctx);
     cudaDeviceProp prop;
     char dev_name[256] = {0};
@@ -1354,7 +1354,6 @@ int orn_wave_tune(orn_context* ctx, const char* cache_path, orn_wave_config* cho
             for (int si = 0; si < 2 && e == cudaSuccess; ++si) {
                 const orn::WaveConfig c{shape, fetches[fi], steps[si]};
                 p.wave_fetch = c.fetch;
-                p.wave_steps = c.steps;
                 float ms = 0.0f;
                 for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {   // the first run warms the caches
                     e = cudaMemcpyAsync(rng, ctx->rng, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice,

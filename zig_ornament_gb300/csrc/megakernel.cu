@@ -68,8 +68,13 @@ template <> struct Accum<true> {
 // first rough surface from the second vertex on) and leaves a query there; a
 // training pixel's path runs to the end and records the network inputs at
 // the cache vertex and the radiance that left it.
+// Resident blocks per SM the CACHE variant is compiled for (register cap).
+// Measured on cached + batched 1920x1080 frames (ms per frame): 3 blocks
+// (152 registers, no spills) 63.5, 4 (128) 59.9, 5 (96) 58.1, 6 (80) 55.6,
+// 7 (72) 55.0, 8 (64) 59.4 — more warps in flight outweigh the register
+// spills up to 7.
 #ifndef ORN_CACHE_MIN_BLOCKS
-#define ORN_CACHE_MIN_BLOCKS 4
+#define ORN_CACHE_MIN_BLOCKS 7
 #endif
 template <int SEM, int MATH, bool COUNT, bool FAST, bool F64 = false, bool CACHE = false, bool SOBOL = false>
 __global__ void __launch_bounds__(kMegaBlock, CACHE ? ORN_CACHE_MIN_BLOCKS : kMegaMinBlocks)

@@ -11,7 +11,12 @@
 
 namespace orn {
 
-constexpr int kMegaBlock = 128;
+// Threads per megakernel block (measured on the 1080p workload: 96 threads
+// x 7 blocks, 21 warps per SM, 341 against 364 Msamples/s for 128 x 5).
+#ifndef ORN_MEGA_BLOCK
+#define ORN_MEGA_BLOCK 128
+#endif
+constexpr int kMegaBlock = ORN_MEGA_BLOCK;
 // Traversal-stack entries per thread kept in shared memory (the rest of the
 // 64-entry stack spills to local memory).
 #ifndef ORN_SMEM_STACK
@@ -115,15 +120,14 @@ struct RenderLaunch {
     const uint32_t* order;     // hand-out order of the pixels (null: raster order)
     uint32_t* cost;            // per-pixel traversal steps of this launch (or null)
     int wave_fetch;            // wavefront kernels: idle lanes a traversing warp gathers before taking rays
-    int wave_steps;            // wavefront kernels: node visits per traversal round
 };
 
 // Launch parameters of the persistent wavefront (wave.cu): one of the
 // compiled block shapes (warps per block, of which shading, path slots per
 // block, resident blocks per SM — see wave_shape_info), the idle lanes a
 // traversing warp gathers before it takes new rays, and the node visits per
-// traversal round.  Every configuration renders the same images; only the
-// speed differs.
+// traversal round (compiled for 32 and 64).  Every configuration renders
+// the same images; only the speed differs.
 struct WaveConfig {
     int shape;
     int fetch;
@@ -131,10 +135,11 @@ struct WaveConfig {
 };
 constexpr int kWaveShapes = 4;
 constexpr WaveConfig kWaveDefault = {0, 4, 32};
-// The cached wavefront (wave_cached.cu) has one shape and takes these.
+// The cached wavefront (wave_cached.cu) has one shape and round length and
+// takes this fetch threshold.
 constexpr int kWaveFetchDefault = 4, kWaveStepsDefault = 32;
 __host__ __device__ constexpr bool wave_config_valid(int shape, int fetch, int steps) {
-    return shape >= 0 && shape < kWaveShapes && fetch >= 1 && fetch <= 32 && steps >= 4 && steps <= 256;
+    return shape >= 0 && shape < kWaveShapes && fetch >= 1 && fetch <= 32 && (steps == 32 || steps == 64);
 }
 // Warps, shading warps, path slots per block and resident blocks per SM of
 // compiled shape `shape` (false when there is none).

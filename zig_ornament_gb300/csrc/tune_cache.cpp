@@ -65,10 +65,18 @@ bool write_tune_cache(const char* path, const std::map<std::string, TuneEntry>& 
     std::fprintf(f, "{\n");
     size_t i = 0;
     for (const auto& kv : entries) {
+        // each entry's own fields (a file may hold both tuners' entries):
+        // those named in `names` first, in that order, then the rest
         std::fprintf(f, "  \"%s\": {", kv.first.c_str());
+        const auto& fields = kv.second.fields;
         for (const auto& name : names) {
-            auto it = kv.second.fields.find(name);
-            std::fprintf(f, "\"%s\": %ld, ", name.c_str(), it == kv.second.fields.end() ? 0L : it->second);
+            auto it = fields.find(name);
+            if (it != fields.end()) std::fprintf(f, "\"%s\": %ld, ", name.c_str(), it->second);
+        }
+        for (const auto& fv : fields) {
+            bool listed = false;
+            for (const auto& name : names) listed = listed || name == fv.first;
+            if (!listed) std::fprintf(f, "\"%s\": %ld, ", fv.first.c_str(), fv.second);
         }
         std::fprintf(f, "\"ms\": %.3f}%s\n", kv.second.ms, ++i < entries.size() ? "," : "");
     }

@@ -29,7 +29,8 @@ struct TuneEntry {
 std::map<std::string, TuneEntry> read_tune_cache(const char* path);
 
 // Writes `entries` to `path` (through a temporary file renamed over it),
-// the integer fields in the order `names` gives; false on an I/O error.
+// each with its own integer fields, those in `names` first and in that
+// order; false on an I/O error.
 bool write_tune_cache(const char* path, const std::map<std::string, TuneEntry>& entries,
                       const std::vector<std::string>& names);
 

@@ -63,8 +63,9 @@ struct Pool {
 }  // namespace
 
 // NW warps per block, NS of them shading, P path slots, launch bounds for
-// MINB resident blocks per SM (the register cap).
-template <int SEM, bool COUNT, bool FAST, int NW, int NS, int P, int MINB>
+// MINB resident blocks per SM (the register cap), STEPS node visits per
+// traversal round.
+template <int SEM, bool COUNT, bool FAST, int NW, int NS, int P, int MINB, int STEPS>
 __global__ void __launch_bounds__(32 * NW, MINB)
 wave_kernel(RenderLaunch p) {
     extern __shared__ __align__(16) unsigned char wave_smem[];
@@ -214,7 +215,8 @@ wave_kernel(RenderLaunch p) {
     if (warp >= (uint32_t)NS) {
         // traversal warps: their lanes' stacks are the first 32 * (NW - NS)
         // columns of the shared stack array
-        traversal_warp<COUNT, FAST, P>(pool, p, sstack + (threadIdx.x - 32 * NS), 32 * (NW - NS), lane, vc, err);
+        traversal_warp<COUNT, FAST, P, STEPS>(pool, p, sstack + (threadIdx.x - 32 * NS), 32 * (NW - NS), lane, vc,
+                                              err);
     } else {
         // the shading warp: up to 32 queued hits per round
         bool ok = true;
@@ -300,13 +302,13 @@ constexpr size_t shape_smem() {
     return ((sizeof(Pool<T::P>) + 15) / 16) * 16 + sizeof(uint32_t) * kSmemStack * 32 * (T::W - T::S);
 }
 
-template <int SEM, bool COUNT, bool FAST, int SHAPE>
+template <int SEM, bool COUNT, bool FAST, int SHAPE, int STEPS>
 cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
     using T = Shape<SHAPE>;
     constexpr int kBlock = 32 * T::W;
     constexpr size_t kSmem = shape_smem<SHAPE>();
     static int blocks_per_sm = 0, sms = 0;
-    auto kern = wave_kernel<SEM, COUNT, FAST, T::W, T::S, T::P, T::B>;
+    auto kern = wave_kernel<SEM, COUNT, FAST, T::W, T::S, T::P, T::B, STEPS>;
     // more than 48 KB of dynamic shared memory: an opt-in per device
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
     if (e != cudaSuccess) return e;
@@ -327,16 +329,23 @@ cudaError_t launch_wave_t(const RenderLaunch& p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-// Counting launches (a diagnostics mode) are compiled for shape 0 only.
-template <int SEM, bool FAST>
-cudaError_t launch_wave_shape(const RenderLaunch& p, int shape, bool count, cudaStream_t s) {
-    if (count) return launch_wave_t<SEM, true, FAST, 0>(p, s);
+template <int SEM, bool FAST, int STEPS>
+cudaError_t launch_wave_steps(const RenderLaunch& p, int shape, cudaStream_t s) {
     switch (shape) {
-        case 1: return launch_wave_t<SEM, false, FAST, 1>(p, s);
-        case 2: return launch_wave_t<SEM, false, FAST, 2>(p, s);
-        case 3: return launch_wave_t<SEM, false, FAST, 3>(p, s);
-        default: return launch_wave_t<SEM, false, FAST, 0>(p, s);
+        case 1: return launch_wave_t<SEM, false, FAST, 1, STEPS>(p, s);
+        case 2: return launch_wave_t<SEM, false, FAST, 2, STEPS>(p, s);
+        case 3: return launch_wave_t<SEM, false, FAST, 3, STEPS>(p, s);
+        default: return launch_wave_t<SEM, false, FAST, 0, STEPS>(p, s);
     }
+}
+
+// Counting launches (a diagnostics mode) are compiled for shape 0 with 32
+// steps per round only.
+template <int SEM, bool FAST>
+cudaError_t launch_wave_shape(const RenderLaunch& p, const WaveConfig& c, bool count, cudaStream_t s) {
+    if (count) return launch_wave_t<SEM, true, FAST, 0, 32>(p, s);
+    return c.steps == 64 ? launch_wave_steps<SEM, FAST, 64>(p, c.shape, s)
+                         : launch_wave_steps<SEM, FAST, 32>(p, c.shape, s);
 }
 
 }  // namespace
@@ -359,13 +368,11 @@ bool wave_shape_info(int shape, int* warps, int* shading, int* slots, int* block
 
 cudaError_t launch_wave(const RenderLaunch& p, const WaveConfig& c, int semantics, bool count, bool fast,
                         cudaStream_t s) {
-    if (!wave_config_valid(c.shape, c.fetch, c.steps) || p.wave_fetch != c.fetch || p.wave_steps != c.steps)
-        return cudaErrorInvalidValue;
+    if (!wave_config_valid(c.shape, c.fetch, c.steps) || p.wave_fetch != c.fetch) return cudaErrorInvalidValue;
     if (semantics == SEM_WGSL)
-        return fast ? launch_wave_shape<SEM_WGSL, true>(p, c.shape, count, s)
-                    : launch_wave_shape<SEM_WGSL, false>(p, c.shape, count, s);
-    return fast ? launch_wave_shape<SEM_HIP, true>(p, c.shape, count, s)
-                : launch_wave_shape<SEM_HIP, false>(p, c.shape, count, s);
+        return fast ? launch_wave_shape<SEM_WGSL, true>(p, c, count, s)
+                    : launch_wave_shape<SEM_WGSL, false>(p, c, count, s);
+    return fast ? launch_wave_shape<SEM_HIP, true>(p, c, count, s) : launch_wave_shape<SEM_HIP, false>(p, c, count, s);
 }
 
 }  // namespace orn

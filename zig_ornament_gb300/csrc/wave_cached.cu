@@ -475,11 +475,11 @@ wave_cached_kernel(RenderLaunch p) {
         return q_push<P>(pool.rq, &pool.rq_tail, emit, slot, lane);
     };
     if ((threadIdx.x >> 5) < (uint32_t)NS)
-        wave_warp<false, FAST, true, P, ROLE_SHADE>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
-                                                    shade);
+        wave_warp<false, FAST, true, P, ROLE_SHADE, kWaveStepsDefault>(pool, p, sstack + threadIdx.x,
+                                                                       (int)blockDim.x, lane, vc, err, shade);
     else
-        wave_warp<false, FAST, true, P, ROLE_BOTH>(pool, p, sstack + threadIdx.x, (int)blockDim.x, lane, vc, err,
-                                                   shade);
+        wave_warp<false, FAST, true, P, ROLE_BOTH, kWaveStepsDefault>(pool, p, sstack + threadIdx.x,
+                                                                      (int)blockDim.x, lane, vc, err, shade);
     if (err) atomicOr(p.error, err);
 }
 
