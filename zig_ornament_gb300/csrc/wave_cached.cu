@@ -65,8 +65,17 @@ __device__ __forceinline__ void st3(float (&a)[3][P], uint32_t i, f3 v) {
 
 }  // namespace
 
+// Resident blocks per SM the kernel is compiled for (register cap).
+// Measured on cached + batched 1920x1080 frames (ms per frame): 2 blocks of
+// 8 warps (128 registers) 64.6; 3 blocks of 8 warps with 192 slots (80
+// registers, 1.6 KB of spills per thread) 102.9; 4 blocks of 6 warps 117.7;
+// 2 blocks of 10 warps 65.8.  Unlike the cached megakernel, spilling the
+// shading code costs more than the extra warps bring.
+#ifndef ORN_WAVE_CACHED_MINB
+#define ORN_WAVE_CACHED_MINB 2
+#endif
 template <int SEM, bool FAST, bool SOBOL, int NW, int NS, int P>
-__global__ void __launch_bounds__(32 * NW, 2)
+__global__ void __launch_bounds__(32 * NW, ORN_WAVE_CACHED_MINB)
 wave_cached_kernel(RenderLaunch p) {
     extern __shared__ __align__(16) unsigned char wave_smem[];
     CPool<P>& pool = *reinterpret_cast<CPool<P>*>(wave_smem);
