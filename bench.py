@@ -535,8 +535,8 @@ def run_ours(args):
                 t_alt = time.perf_counter()
                 alt_bvh = ornament.Bvh(scene, builder=alt)
                 t_alt = time.perf_counter() - t_alt
-                m = measure_megakernel(alt_bvh, scene, args.width, args.height, args.spp, args.depth,
-                                       args.steps, args.warmup, local, flush)
+                m = measure_render(alt_bvh, scene, args.width, args.height, args.spp, args.depth,
+                                   args.steps, args.warmup, local, flush)
                 line[key] = {"value": m["value"], "unit": UNIT, "bvh_build_s": round(t_alt, 3),
                              "note": f"same steps on the {TREE_DESC[alt]} tree: images equal to the "
                                      "reference's in expectation only"}
@@ -546,8 +546,8 @@ def run_ours(args):
         # the same steps on the persistent wavefront (same images), with the
         # launch parameters its autotuner picks for this workload
         try:
-            m = measure_megakernel(bvh, scene, args.width, args.height, args.spp, args.depth, args.steps,
-                                   args.warmup, local, flush, kernel="wavefront")
+            m = measure_render(bvh, scene, args.width, args.height, args.spp, args.depth, args.steps,
+                               args.warmup, local, flush, kernel="wavefront")
             line["wavefront"] = {"value": m["value"], "unit": UNIT, "vs_megakernel": m["value"] / value,
                                  "ms_per_step": m["ms_per_step"], "launches_per_step": m["launches_per_step"],
                                  "wave_config": m["wave_config"],
@@ -596,7 +596,7 @@ def port_speed_note():
     return note
 
 
-def measure_megakernel(bvh, scene, w, h, spp, depth, steps, warmup, local, flush, counters=False, kernel="mega"):
+def measure_render(bvh, scene, w, h, spp, depth, steps, warmup, local, flush, counters=False, kernel="mega"):
     """Device time of `steps` renders of `spp` passes (L2 flushed between
     them); returns Msamples/s, ms per step, launches per step and, with
     `counters`, the exact work of one more (untimed) render.  kernel
@@ -662,8 +662,8 @@ def other_configs(args, local, flush):
             a.workload, a.width, a.height, a.spp, a.depth = wl, None, None, None, None
             a = apply_workload_defaults(a)
             scene, bvh, cfg = workload(a)
-            m = measure_megakernel(bvh, scene, a.width, a.height, a.spp, a.depth, steps, warmup, local, flush,
-                                   counters=True)
+            m = measure_render(bvh, scene, a.width, a.height, a.spp, a.depth, steps, warmup, local, flush,
+                               counters=True)
             c = m["counters"]
             launch_s = m["ms_per_step"] / 1e3 / max(m["launches_per_step"], 1)
             bpl = algorithmic_bytes(c) / max(m["launches_per_step"], 1)
