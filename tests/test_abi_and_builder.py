@@ -29,6 +29,21 @@ def test_library_exports_every_declared_function():
     assert set(declared) == set(_lib.FUNCTIONS), set(declared) ^ set(_lib.FUNCTIONS)
 
 
+def test_integration_bindings_call_declared_functions():
+    """The Zig and C snippets a maintainer copies from INTEGRATION.md call
+    only functions the header declares (and every declared function is
+    named there or in the header's own documentation)."""
+    text = (ROOT / "INTEGRATION.md").read_text()
+    used = set(re.findall(r"\bc\.(orn_[a-z0-9_]+)\s*\(", text)) | set(re.findall(r"`(orn_[a-z0-9_]+)", text))
+    declared = set(header_functions())
+    header = (ROOT / "include" / "ornament_cuda.h").read_text()
+    types = set(re.findall(r"\b(?:struct|enum)\s+(orn_[a-z0-9_]+)", header)) | {"orn_headless"}   # + the C driver
+    # `orn_batch_*` style mentions name a family, not a function
+    unknown = {u for u in used if u not in declared and u not in types and not u.endswith("_")}
+    assert not unknown, unknown
+    assert len(used & declared) >= 20
+
+
 def test_struct_sizes_match_gpu_structs_zig():
     assert C.sizeof(_lib.BvhNode) == 64
     assert C.sizeof(_lib.Material) == 32
